@@ -1,0 +1,86 @@
+// engine.h — internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/axicor_day.h"
+
+namespace axc {
+
+// Control block of one shard in device memory.
+struct ShardCtl {
+  uint32_t spike_count;   // spikers listed by the last update stage
+  uint32_t err;           // AXC_ERR_* bits, sticky until read with clear
+  uint32_t tick_base;     // batch mode: global tick of tick 0 of the batch
+  int32_t dopamine;       // batch mode: dopamine of the batch
+  uint32_t pad[4];
+  unsigned long long ctr[8];  // statistics, see axc_shard_counters
+};
+
+// Per-shard scratch owned by the engine, next to the reference-visible
+// state.  Sized for (padded_n, total_axons).
+struct ShardScratch {
+  uint32_t padded_n = 0;
+  uint32_t total_axons = 0;
+  void* base = nullptr;        // single allocation
+  uint32_t* seg_mask = nullptr;  // [A] segment-hit mask of the propagated heads
+  uint32_t* pend = nullptr;      // [A] soma pushes pending for the push stage
+  uint32_t* incoming = nullptr;  // [A] network spike pushes pending for the axon stage
+  uint32_t* spikers = nullptr;   // [N] ids of the neurons that spiked this tick
+  ShardCtl* ctl = nullptr;
+  uint32_t* batch_counts = nullptr;  // [batch_cap] per-tick network spike counts
+  uint32_t batch_cap = 0;
+  uint32_t* h_counts_pinned = nullptr;  // pinned staging for batch_counts / tick_base
+  void* graph_cache = nullptr;          // batch engine graphs (batch_engine.cu)
+};
+
+// Registry keyed by the axon_heads pointer.  Created by cu_allocate_shard;
+// created lazily (and sized) for shards whose memory the caller allocated.
+ShardScratch* scratch_for(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons,
+                          cudaError_t* err);
+void scratch_release(const void* heads_key);
+void graph_cache_free(ShardScratch* s);  // batch_engine.cu
+
+// Tick stages (day_phase.cu).  When dctl_batch is true the tick number,
+// dopamine and network spike count come from the shard's device control
+// block (tick = ctl->tick_base + k, count = batch_counts[k]).
+struct TickArgs {
+  uint32_t padded_n, total_axons, v_seg, tick;
+  const uint32_t* input_bitmask;
+  uint32_t virtual_offset, num_virtual;
+  const uint32_t* incoming_spikes;
+  uint32_t num_incoming;      // per-tick mode
+  uint32_t max_incoming;      // batch mode: capacity of the tick's schedule row
+  const uint32_t* mapped_soma_ids;
+  uint8_t* output_history;
+  uint32_t num_outputs;
+  int16_t dopamine;
+  bool batch;                 // read tick/dopamine/count from the device control block
+  uint32_t k;                 // tick index inside the batch
+};
+
+// ev (optional): 6 events recorded around the stages (incoming, axons,
+// update, push, gsop) for per-kernel timing.
+constexpr int kTickStages = 5;
+cudaError_t launch_tick(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
+                        cudaEvent_t* ev = nullptr);
+cudaError_t launch_reset_burst(const ShardVramPtrs& v, uint32_t padded_n, cudaStream_t stream);
+cudaError_t launch_spike_list_sorted(const ShardVramPtrs& v, uint32_t padded_n, uint32_t* out_ids,
+                                     uint32_t* out_count, cudaStream_t stream);
+
+// Stand-alone stages for the legacy per-kernel launchers (ffi.rs:193-233).
+cudaError_t launch_push_incoming(BurstHeads8* heads, ShardScratch& s, uint32_t A, const uint32_t* ids,
+                                 uint32_t count, cudaStream_t stream);
+cudaError_t launch_propagate_only(BurstHeads8* heads, uint32_t A, uint32_t v_seg, cudaStream_t stream);
+cudaError_t launch_update_stage(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, uint32_t tick,
+                                cudaStream_t stream);
+cudaError_t launch_gsop_stage(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, int16_t dopamine,
+                              cudaStream_t stream);
+
+// LUT access for host code (day_phase.cu owns the __constant__ symbol).
+cudaError_t lut_upload(const VariantParameters* lut, cudaStream_t stream, bool async);
+
+int sm_count();
+
+}  // namespace axc

@@ -1,0 +1,415 @@
+#!/usr/bin/env python3
+"""Day Phase benchmark: synaptic events/s and ticks/s of one seeded brain.
+
+Default workload: 1,507,328 integer GLIF neurons on a 128x128x92 grid, 100
+dendrite slots each (150.7M synapses), 4,096 Bernoulli inputs at p=0.05,
+GSOP on.  One step = one batch of `--ticks-per-step` ticks through the
+engine's batch entry point (CUDA-graph replay of the tick loop).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Synaptic events/s = ticks/s x non-empty dendrite slots (the reference's own
+definition, examples/cartpole_exp/benchmark.py:112).  `value` is measured
+with the batch's inputs already in device memory; `e2e` through the same
+public call with pinned host inputs and a device-to-host read of the output
+readout every step.  `--impl reference` times the CPU restatement of the
+reference kernels (the reference has no CPU Day Phase of its own) on the
+host cores.  With N > 1 (torchrun), every rank runs an independent replica.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CONFIGS = {"plain-1.5M": "config1", "plain-16k": "config0", "plain-8M": "config4"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="plain-1.5M", choices=sorted(CONFIGS))
+    ap.add_argument("--ticks-per-step", type=int, default=100)
+    ap.add_argument("--outputs", type=int, default=4096)
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self, n_gpus: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            backend = os.environ.get("AXC_BENCH_BACKEND", "gloo")
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("AXC_CLOCKS_CSV", f"/tmp/axc_clocks_{os.getpid()}.csv"))
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines()[1:]:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1].split()[0]))
+                smax.append(float(parts[2].split()[0]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def workload(name: str):
+    from axicor_gb300 import workloads as W
+    return getattr(W, CONFIGS[name])()
+
+
+def synapse_count(state: np.ndarray, padded_n: int) -> int:
+    from axicor_gb300.formats import StateView
+    return int(np.count_nonzero(StateView(state, padded_n).targets))
+
+
+def algorithmic_bytes(ticks, evaluated, spikes, gsop_slots, N, A, I, num_outputs):
+    """Bytes a tick must move (per the Day Phase's data flow):
+    6 B per evaluated slot (u32 target + i16 weight), 64 B per axon (heads read
+    and written), 20 B per neuron (voltage and threshold r/w 16 B, flags and
+    timer r/w 4 B), 4 B per spike (soma_to_axon), 8 B per GSOP slot (target
+    re-read, weight read and written), 4 B per input word and 6 B per output."""
+    return (6 * evaluated + ticks * (64 * A + 20 * N + 4 * ((I + 31) // 32) + 6 * num_outputs)
+            + 4 * spikes + 8 * gsop_slots)
+
+
+def update_kernel_bytes(ticks, evaluated, spikes, N):
+    """Algorithmic bytes of the update kernel: 6 B per evaluated slot, 20 B per neuron, 4 B per spike."""
+    return 6 * evaluated + ticks * 20 * N + 4 * spikes
+
+
+def run_gb300(args, dist: Dist) -> dict | None:
+    import __graft_entry__ as G
+    G.build()
+    from axicor_gb300 import _native as N
+    from axicor_gb300 import shard as S
+
+    lib = N.lib()
+    lib.gpu_set_device(dist.local_rank)
+    w = workload(args.workload)
+    B, K, Wm = args.ticks_per_step, args.steps, args.warmup
+    lay, state, heads = S.generate_brain(w.spec())
+    synapses = synapse_count(state, lay.padded_n)
+    S.upload_lut(w.lut)
+    vram = S.VramState(lay.padded_n, lay.total_axons)
+    vram.upload_state(state)
+    vram.upload_axon_heads(heads)
+    del heads
+    eng = S.ShardEngine(vram)
+    words = (w.num_inputs + 31) // 32
+    n_out = min(args.outputs, lay.num_neurons)
+    ids = np.linspace(0, lay.num_neurons - 1, n_out).astype(np.uint32)
+    d_ids = S.device_array(ids)
+    io = S.IoDeviceBuffers(words, 0, n_out, B)
+
+    total_ticks = (Wm + 2 * K) * B
+    bm_all = S.input_bitmask(w.seed, 0, total_ticks, w.num_inputs, w.rate_q32)
+    d_bm_all = S.device_array(bm_all)
+    tick = 0
+
+    def step_device(t0):
+        src = d_bm_all + t0 * words * 4
+        err = lib.axc_step_day_phase_batch(C.byref(vram.ptrs), lay.padded_n, lay.total_axons, B,
+                                           C.byref(io.as_struct()), src, None, None, lay.virtual_offset,
+                                           w.num_inputs, d_ids, w.v_seg, w.dopamine, t0, None, eng.stream)
+        if err:
+            raise RuntimeError(f"axc_step_day_phase_batch failed: {err}")
+
+    for _ in range(Wm):
+        step_device(tick)
+        tick += B
+    eng.synchronize()
+
+    import torch
+    torch.cuda.set_device(dist.local_rank)
+    stream = torch.cuda.ExternalStream(eng.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    vram.counters(reset=True)
+    clocks = Clocks(dist.local_rank)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    for _ in range(K):
+        step_device(tick)
+        tick += B
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    ctr = vram.counters()
+    t_max = dist.max(ms / 1e3)
+    ticks_timed = K * B
+    value_tps = dist.world * ticks_timed / t_max
+
+    # e2e: pinned host inputs and a host read of the readout, through the same call
+    h_bm = S.PinnedBuffer(K * B * words, np.uint32)
+    h_bm.array[:] = bm_all[tick * words:(tick + K * B) * words]
+    h_out = S.PinnedBuffer(B * n_out, np.uint8)
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    wall0 = time.perf_counter()
+    e0.record(stream)
+    for k in range(K):
+        src = h_bm.as_ptr() + k * B * words * 4
+        err = lib.axc_step_day_phase_batch(C.byref(vram.ptrs), lay.padded_n, lay.total_axons, B,
+                                           C.byref(io.as_struct()), src, None, None, lay.virtual_offset,
+                                           w.num_inputs, d_ids, w.v_seg, w.dopamine, tick, h_out.as_ptr(),
+                                           eng.stream)
+        if err:
+            raise RuntimeError(f"axc_step_day_phase_batch (e2e) failed: {err}")
+        tick += B
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    e2e_s = dist.max(max(e0.elapsed_time(e1) / 1e3, wall))
+    e2e_tps = dist.world * K * B / e2e_s
+
+    # per-kernel CUDA-event timing on the launching stream (same regime, right after)
+    prof_ticks = min(50, B)
+    out_ms = (C.c_float * 5)()
+    out_cnt = (C.c_uint64 * 4)()
+    d_prof_bm = S.device_array(bm_all[:prof_ticks * words])
+    err = lib.axc_profile_ticks(C.byref(vram.ptrs), lay.padded_n, lay.total_axons, w.v_seg, tick, prof_ticks,
+                                d_prof_bm, words, lay.virtual_offset, w.num_inputs, w.dopamine, eng.stream, out_ms,
+                                out_cnt)
+    if err:
+        raise RuntimeError(f"axc_profile_ticks failed: {err}")
+    stage_ms = list(out_ms)
+    names = ["network_ids", "axons", "update", "push", "gsop"]
+    top = int(np.argmax(stage_ms))
+    ev, hits, spk, gs = (int(x) for x in out_cnt)
+    if names[top] == "update":
+        kb = update_kernel_bytes(prof_ticks, ev, spk, lay.padded_n)
+    elif names[top] == "gsop":
+        kb = 8 * gs
+    elif names[top] == "axons":
+        kb = prof_ticks * (64 * lay.total_axons + 4 * lay.total_axons)
+    else:
+        kb = 4 * spk
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = kb / (stage_ms[top] / 1e3) / 1e9
+    tick_bytes = algorithmic_bytes(ticks_timed, int(ctr[1]), int(ctr[3]), int(ctr[4]), lay.padded_n,
+                                   lay.total_axons, w.num_inputs, n_out)
+
+    result = {
+        "ticks_per_s": value_tps,
+        "events_per_s": value_tps * synapses,
+        "e2e_events_per_s": e2e_tps * synapses,
+        "e2e_ticks_per_s": e2e_tps,
+        "ms_per_step": t_max * 1e3 / K,
+        "synapses": synapses,
+        "neurons": lay.num_neurons,
+        "clocks": clk,
+        "h2d": B * words * 4,
+        "d2h": B * n_out,
+        "launches": K * (4 * B + 2),
+        "roofline": {"bound": "hbm", "kernel": f"k_update" if names[top] == "update" else f"k_{names[top]}",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+        "stage_ms_per_tick": {n: m / prof_ticks for n, m in zip(names, stage_ms)},
+        "tick_algorithmic_gbs": tick_bytes / (ms / 1e3) / 1e9,
+        "per_tick": {"evaluated_slots": int(ctr[1]) / ticks_timed, "hits": int(ctr[2]) / ticks_timed,
+                     "spikes": int(ctr[3]) / ticks_timed, "gsop_slots": int(ctr[4]) / ticks_timed},
+        "delivered_events_per_s": value_tps * int(ctr[2]) / ticks_timed,
+        "lay": lay, "w": w, "vram": vram,
+    }
+    lib.gpu_free(d_ids)
+    lib.gpu_free(d_bm_all)
+    lib.gpu_free(d_prof_bm)
+    return result
+
+
+def cpu_sample(w, state, heads, lay, tick0, budget_s, threads) -> dict:
+    """Times the CPU restatement of the reference kernels on `threads` host threads."""
+    import oracle
+    words = (w.num_inputs + 31) // 32
+    t_once = None
+    ticks = 0
+    t0 = time.perf_counter()
+    while True:
+        bm = __import__("axicor_gb300.shard", fromlist=["x"]).input_bitmask(w.seed, tick0 + ticks, 1, w.num_inputs,
+                                                                             w.rate_q32)
+        s = time.perf_counter()
+        oracle.run_ticks(state, heads, w.lut, lay.padded_n, lay.total_axons, w.v_seg, tick0 + ticks, 1, bm, words,
+                         lay.virtual_offset, w.num_inputs, threads=threads)
+        ticks += 1
+        t_once = time.perf_counter() - s
+        if time.perf_counter() - t0 + t_once > budget_s or ticks >= 200:
+            break
+    el = time.perf_counter() - t0
+    return {"ticks": ticks, "seconds": el, "ticks_per_s": ticks / el}
+
+
+def run_reference(args, dist: Dist) -> None:
+    """CPU arm: the oracle (a C restatement of physics.cu) on all host cores."""
+    if dist.rank != 0:
+        return
+    import oracle
+    from axicor_gb300 import shard as S
+    import __graft_entry__ as G
+    G.build()
+    w = workload(args.workload)
+    lay, state, heads = S.generate_brain(w.spec())
+    synapses = synapse_count(state, lay.padded_n)
+    threads = os.cpu_count() or 1
+    words = (w.num_inputs + 31) // 32
+    pre = 16                      # untimed ticks that bring the brain to its steady activity
+    bm = S.input_bitmask(w.seed, 0, pre, w.num_inputs, w.rate_q32)
+    oracle.run_ticks(state, heads, w.lut, lay.padded_n, lay.total_axons, w.v_seg, 0, pre, bm, words,
+                     lay.virtual_offset, w.num_inputs, threads=threads)
+    tick = pre
+    per_step = 1
+    for _ in range(args.warmup):
+        bm = S.input_bitmask(w.seed, tick, per_step, w.num_inputs, w.rate_q32)
+        oracle.run_ticks(state, heads, w.lut, lay.padded_n, lay.total_axons, w.v_seg, tick, per_step, bm, words,
+                         lay.virtual_offset, w.num_inputs, threads=threads)
+        tick += per_step
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bm = S.input_bitmask(w.seed, tick, per_step, w.num_inputs, w.rate_q32)
+        oracle.run_ticks(state, heads, w.lut, lay.padded_n, lay.total_axons, w.v_seg, tick, per_step, bm, words,
+                         lay.virtual_offset, w.num_inputs, threads=threads)
+        tick += per_step
+    el = time.perf_counter() - t0
+    tps = args.steps * per_step / el
+    v = tps * synapses
+    line = {
+        "metric": "synaptic_events_per_s", "value": v, "unit": "events/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator)", "ticks_per_s": tps,
+        "config": {"workload": args.workload, "neurons": lay.num_neurons, "synapses": synapses,
+                   "ticks_per_step": per_step, "pre_ticks_untimed": pre, "parallelism": "replicas"},
+        "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} ticks of the {args.workload} brain after {pre + args.warmup} "
+                                   f"untimed ticks, C restatement of physics.cu with OpenMP"},
+        "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+            return
+        r = run_gb300(args, dist)
+        if dist.rank != 0:
+            return
+        cpu = None
+        if not args.no_cpu_baseline and dist.world == 1:
+            import oracle  # noqa: F401  (the checker doubles as the timed CPU baseline)
+            vram, lay, w = r["vram"], r["lay"], r["w"]
+            st, hd = vram.download_state(), vram.download_heads()
+            threads = os.cpu_count() or 1
+            cs = cpu_sample(w, st, hd, lay, 10 ** 6, args.cpu_sample_s, threads)
+            cpu = {"value": cs["ticks_per_s"] * r["synapses"], "unit": "events/s", "cores": threads, "kind": "port",
+                   "sample": f"{cs['ticks']} ticks ({cs['seconds']:.1f} s) of the {args.workload} brain from the "
+                             f"GPU's state after the timed region; C restatement of physics.cu, OpenMP",
+                   "ticks_per_s": cs["ticks_per_s"]}
+        line = {
+            "metric": "synaptic_events_per_s", "value": r["events_per_s"], "unit": "events/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded generator, inputs resident in HBM)",
+            "ticks_per_s": r["ticks_per_s"],
+            "delivered_events_per_s": r["delivered_events_per_s"],
+            "config": {"workload": args.workload, "neurons": r["neurons"], "synapses": r["synapses"],
+                       "ticks_per_step": args.ticks_per_step, "parallelism": "replicas" if dist.world > 1 else "single",
+                       "l2": "inputs larger than L2 (1.37 GB .state per brain)", "gsop": True},
+            "e2e": {"value": r["e2e_events_per_s"], "unit": "events/s", "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"], "ticks_per_s": r["e2e_ticks_per_s"]},
+            "gpu_launches": r["launches"],
+            "roofline": r["roofline"],
+            "tick_algorithmic_gbs": r["tick_algorithmic_gbs"],
+            "stage_ms_per_tick": r["stage_ms_per_tick"],
+            "per_tick": r["per_tick"],
+            "clocks": r["clocks"],
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,326 @@
+/*
+ * axicor_day.h — C-ABI of the GB300 Day Phase engine.
+ *
+ * The first half of this header is the drop-in boundary: the same unmangled
+ * symbols, argument orders and #[repr(C)] layouts that the Rust crate
+ * genesis-compute binds in genesis-compute/src/ffi.rs:27-273 (link name
+ * "genesis_cuda", ffi.rs:48).  A Rust build links this library in place of
+ * the reference's physics.cu + bindings.cu without source changes.
+ *
+ * The second half (axc_* symbols) is new: a batch API with a CUDA-graph
+ * captured tick loop, spike compaction, device error reporting, and the
+ * brain generator used to build the synthetic benchmark brains.
+ *
+ * Conventions
+ *  - A "stream" argument is a cudaStream_t passed as an opaque pointer
+ *    (Rust: CudaStream = *mut c_void, ffi.rs:5).  NULL is the legacy stream.
+ *  - int32_t returns are cudaError_t values (0 = success) unless stated.
+ *  - Every pointer inside ShardVramPtrs is a device pointer.
+ */
+#ifndef AXICOR_DAY_H
+#define AXICOR_DAY_H
+
+#include <stddef.h>
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AXC_MAX_DENDRITES 128u     /* genesis-core/src/constants.rs:9        */
+#define AXC_AXON_SENTINEL 0x80000000u /* constants.rs:13                    */
+#define AXC_TARGET_AXON_MASK 0x00FFFFFFu /* constants.rs:20                 */
+#define AXC_TARGET_SEG_SHIFT 24u   /* constants.rs:21                        */
+#define AXC_NO_AXON 0xFFFFFFFFu    /* soma_to_axon / mapped_soma_ids "none"  */
+
+/* Eight-slot burst shift register of one axon (genesis-core/src/layout.rs:53-74). */
+typedef struct __attribute__((aligned(32))) BurstHeads8 {
+  uint32_t h0, h1, h2, h3, h4, h5, h6, h7;
+} BurstHeads8;
+
+/* Neuron-type parameters, 64 bytes (genesis-core/src/layout.rs:12-48). */
+typedef struct __attribute__((aligned(64))) VariantParameters {
+  int32_t threshold;                        /*  0 */
+  int32_t rest_potential;                   /*  4 */
+  int32_t leak_rate;                        /*  8 */
+  int32_t homeostasis_penalty;              /* 12 */
+  uint32_t spontaneous_firing_period_ticks; /* 16 */
+  uint16_t initial_synapse_weight;          /* 20 */
+  uint16_t gsop_potentiation;               /* 22 */
+  uint16_t gsop_depression;                 /* 24 */
+  uint16_t homeostasis_decay;               /* 26 */
+  uint8_t refractory_period;                /* 28 */
+  uint8_t synapse_refractory_period;        /* 29 */
+  uint8_t signal_propagation_length;        /* 30 */
+  uint8_t is_inhibitory;                    /* 31 */
+  uint8_t inertia_curve[16];                /* 32 */
+  int32_t adaptive_leak_max;                /* 48 */
+  uint16_t adaptive_leak_gain;              /* 52 */
+  uint8_t adaptive_mode;                    /* 54 */
+  uint8_t _leak_pad[3];                     /* 55 */
+  uint8_t d1_affinity;                      /* 58 */
+  uint8_t d2_affinity;                      /* 59 */
+  uint8_t _pad[4];                          /* 60 */
+} VariantParameters;
+
+/* Device pointers of one shard, field order == .state blob order
+ * (genesis-compute/src/ffi.rs:25-42, memory.rs:71-86). */
+typedef struct ShardVramPtrs {
+  int32_t* soma_voltage;      /* [N]        base of the state allocation */
+  uint8_t* soma_flags;        /* [N]        [7:4] variant, [3:1] burst, [0] spike */
+  int32_t* threshold_offset;  /* [N] */
+  uint8_t* timers;            /* [N]        refractory countdown */
+  uint32_t* soma_to_axon;     /* [N] */
+  uint32_t* dendrite_targets; /* [128][N]   (seg<<24) | (axon+1) */
+  int16_t* dendrite_weights;  /* [128][N] */
+  uint8_t* dendrite_timers;   /* [128][N]   not touched by the Day Phase */
+  BurstHeads8* axon_heads;    /* [A]        separate allocation */
+} ShardVramPtrs;
+
+/* Legacy by-value state of the old per-kernel launchers (genesis-core/src/layout.rs:281-307). */
+typedef struct VramState {
+  uint32_t padded_n;
+  uint32_t total_axons;
+  int32_t* voltage;
+  uint8_t* flags;
+  int32_t* threshold_offset;
+  uint8_t* refractory_timer;
+  uint32_t* soma_to_axon;
+  uint32_t* dendrite_targets;
+  int16_t* dendrite_weights;
+  uint8_t* dendrite_timers;
+  BurstHeads8* axon_heads;
+  uint32_t* input_bitmask;
+  uint8_t* output_history;
+  uint32_t* telemetry_count;
+  uint32_t* telemetry_spikes;
+} VramState;
+
+/* Inter-node spike message record (genesis-core/src/ipc.rs:395-403, bindings.cu:371-374). */
+typedef struct __attribute__((packed)) SpikeEvent {
+  uint32_t ghost_id;
+  uint32_t tick_offset;
+} SpikeEvent;
+
+/* ===================================================================== */
+/* Drop-in boundary: genesis-compute/src/ffi.rs                           */
+/* ===================================================================== */
+
+/* ffi.rs:57 / bindings.cu:571-631.  One zero-filled state allocation sliced
+ * in blob order, one heads allocation filled with the sentinel. */
+int32_t cu_allocate_shard(uint32_t padded_n, uint32_t total_axons, ShardVramPtrs* out_vram);
+
+/* ffi.rs:63 / physics.cu:497-501.  flags &= 0xF1 on the stream. */
+void cu_reset_burst_counters(const ShardVramPtrs* ptrs, uint32_t padded_n, void* stream);
+
+/* ffi.rs:72 / bindings.cu:638-653.  Synchronous copy of the whole .state blob. */
+int32_t cu_upload_state_blob(const ShardVramPtrs* vram, const void* state_blob, size_t state_size);
+
+/* ffi.rs:80 / bindings.cu:658-669.  Synchronous copy of a .axons blob (may be
+ * shorter than total_axons; the rest keeps its sentinel fill). */
+int32_t cu_upload_axons_blob(const ShardVramPtrs* vram, const void* axons_blob, size_t axons_size);
+
+/* ffi.rs:87 / bindings.cu:675-692.  Frees both allocations, nulls the pointers. */
+void cu_free_shard(ShardVramPtrs* vram);
+
+/* ffi.rs:90-106 / physics.cu:441-495.  One Day Phase tick, asynchronous on
+ * `stream`.  NULL pointers / zero counts skip the input, network and readout
+ * stages.  Returns the launch status (the reference always returned 0). */
+int32_t cu_step_day_phase(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons,
+                          uint32_t v_seg, uint32_t current_tick, const uint32_t* input_bitmask,
+                          uint32_t virtual_offset, uint32_t num_virtual_axons,
+                          const uint32_t* incoming_spikes, uint32_t num_incoming_spikes,
+                          const uint32_t* mapped_soma_ids, uint8_t* output_history,
+                          uint32_t num_outputs, int16_t dopamine, void* stream);
+
+/* ffi.rs:109 / physics.cu:504-506.  Synchronous upload of the 16-entry LUT
+ * shared by every shard in the process. */
+int32_t cu_upload_constant_memory(const VariantParameters* lut);
+
+/* ffi.rs:114-154 / bindings.cu:214-265.  Memory and stream helpers. */
+void* gpu_malloc(size_t size);
+void gpu_free(void* dev_ptr);
+void* gpu_host_alloc(size_t size);
+void gpu_host_free(void* ptr);
+void gpu_memcpy_host_to_device_async(void* dst, const void* src, size_t size, void* stream);
+void gpu_memcpy_device_to_host_async(void* dst, const void* src, size_t size, void* stream);
+bool gpu_memcpy_host_to_device(void* dst_dev, const void* src_host, size_t size);
+/* ffi.rs:140-144 declares bool; bindings.cu:248 defined void.  bool here. */
+bool gpu_memcpy_device_to_host(void* dst_host, const void* src_dev, size_t size);
+int32_t gpu_stream_create(void** out_stream); /* non-blocking stream, bindings.cu:257-259 */
+int32_t gpu_stream_destroy(void* stream);
+void gpu_stream_synchronize(void* stream);
+void gpu_set_device(int32_t device_id);
+void gpu_device_synchronize(void);
+void gpu_synchronize(void);
+
+/* ffi.rs:157-158 / bindings.cu:267-282.  LUT uploads (1024 bytes). */
+void gpu_load_constants(const void* host_ptr);
+void update_constant_memory_hot_reload(const VariantParameters* new_variants, void* stream);
+
+/* ffi.rs:160-164 / bindings.cu:450-515,699-710.  Night Phase sort-and-prune
+ * of every neuron's 128 slots (legacy stream, asynchronous). */
+void launch_sort_and_prune(const ShardVramPtrs* ptrs, uint32_t padded_n, int16_t prune_threshold);
+
+/* ffi.rs:166-176 / bindings.cu:378-436.  Emits one SpikeEvent per head born
+ * inside the last `sync_batch_ticks` ticks of each boundary axon.  Resets
+ * *out_count first.  Events are written in (axon order, head order) — a
+ * deterministic order; the reference's atomic order was not. */
+void launch_extract_outgoing_spikes(const BurstHeads8* axon_heads, const uint32_t* src_indices,
+                                    const uint32_t* dst_ghost_ids, uint32_t count,
+                                    uint32_t sync_batch_ticks, uint32_t v_seg, void* out_events,
+                                    uint32_t* out_count, void* stream);
+
+/* ffi.rs:178-185 / bindings.cu:341-368.  dst[dst_idx[i]] = src[src_idx[i]]
+ * for src_idx < 2^31. */
+void launch_ghost_sync(const BurstHeads8* src_heads, BurstHeads8* dst_heads,
+                       const uint32_t* src_indices, const uint32_t* dst_indices, uint32_t count,
+                       void* stream);
+
+/* ffi.rs:193-233 / bindings.cu:106-207,295-334.  Legacy per-kernel launchers
+ * on the legacy stream, kept linkable.  launch_update_neurons and
+ * launch_apply_gsop are declared by ffi.rs:215-224 but defined nowhere in the
+ * reference; here they run the same update / GSOP stages as cu_step_day_phase
+ * (constants_ptr is ignored: the process LUT is used). */
+void launch_inject_inputs(VramState vram, const uint32_t* bitmask, uint32_t current_tick,
+                          uint32_t total_virtual_axons);
+void launch_apply_spike_batch(VramState vram, const uint32_t* tick_schedule,
+                              uint32_t tick_spikes_count);
+void launch_propagate_axons(VramState vram, uint32_t v_seg);
+void launch_update_neurons(VramState vram, const void* constants_ptr, uint32_t current_tick);
+void launch_apply_gsop(VramState vram);
+void launch_record_readout(VramState vram, const uint32_t* mapped_soma_ids, uint8_t* output_history,
+                           uint32_t current_tick, uint32_t total_pixels);
+
+/* ffi.rs:235-246 / bindings.cu:780-796, physics.cu:400-434.  Ballot/popc
+ * compaction of the spiking soma ids into out_ids; *out_count is incremented
+ * (the caller resets it, gpu_reset_telemetry_count resets the count of the
+ * shard's internal list only).  Ids are written in ascending order. */
+void gpu_reset_telemetry_count(const ShardVramPtrs* ptrs, void* stream);
+void launch_extract_telemetry(const ShardVramPtrs* ptrs, uint32_t padded_n, uint32_t* out_ids,
+                              uint32_t* out_count_pinned, void* stream);
+
+/* ffi.rs:248-272 / bindings.cu:717-778.  Per-batch I/O buffers. */
+int32_t cu_allocate_io_buffers(uint32_t input_words, uint32_t schedule_capacity,
+                               uint32_t output_capacity, uint32_t** d_input_bitmask,
+                               uint32_t** d_incoming_spikes, uint8_t** d_output_history);
+int32_t cu_dma_h2d_io(uint32_t* d_input_bitmask, const uint32_t* h_input_bitmask,
+                      uint32_t input_words, uint32_t* d_incoming_spikes,
+                      const uint32_t* h_incoming_spikes, uint32_t schedule_capacity,
+                      void* stream);
+int32_t cu_dma_d2h_io(uint8_t* h_output_history, const uint8_t* d_output_history,
+                      uint32_t output_capacity, void* stream);
+
+/* ===================================================================== */
+/* New entry points (axc_*)                                               */
+/* ===================================================================== */
+
+/* Error bits a tick can raise on the device.  The reference reads or writes
+ * out of bounds in each of these cases; here the access is skipped, the bit
+ * is set, and the host reads it with axc_shard_error_flags. */
+#define AXC_ERR_TARGET_RANGE   0x1u /* dendrite target axon id >= total_axons or field 0 */
+#define AXC_ERR_SOMA_AXON      0x2u /* soma_to_axon >= total_axons (and not 0xFFFFFFFF)  */
+#define AXC_ERR_VIRTUAL_RANGE  0x4u /* virtual_offset + num_virtual_axons > total_axons   */
+#define AXC_ERR_READOUT_RANGE  0x8u /* mapped_soma_id >= padded_n (and not 0xFFFFFFFF)   */
+
+/* Library version string. */
+const char* axc_version(void);
+
+/* Reads (and with clear != 0, clears) the error bits of a shard.  Synchronous. */
+int32_t axc_shard_error_flags(const ShardVramPtrs* vram, uint32_t clear, uint32_t* out_flags);
+
+/* Device spike list of the last tick of a shard: count and ascending ids.
+ * out_ids may be NULL to read only the count.  Synchronous on `stream`. */
+int32_t axc_last_spikes(const ShardVramPtrs* vram, uint32_t* out_count, uint32_t* out_ids,
+                        uint32_t capacity, void* stream);
+
+/* Batch engine: mirror of ShardEngine::step_day_phase_batch
+ * (genesis-compute/src/compute/shard.rs:40-124).  Copies the batch's host
+ * inputs (bitmask words_per_tick x batch, spike schedule max_spikes x batch)
+ * into the device I/O buffers, resets the burst counters, then runs
+ * `batch` ticks with global tick = tick_base + k.  The tick loop is captured
+ * once into a CUDA graph per (shard, batch shape) and replayed.
+ * h_output_history, when not NULL, receives num_outputs x batch bytes
+ * (device to host on the stream).  h_spike_counts may be NULL (no network
+ * spikes).  Asynchronous on `stream` unless h_output_history is given, in
+ * which case the call returns after the output copy completed. */
+typedef struct AxcIoBuffers {
+  uint32_t* d_input_bitmask;
+  uint32_t* d_incoming_spikes;
+  uint8_t* d_output_history;
+  uint32_t max_spikes_per_tick;
+  uint32_t input_words_per_tick;
+  uint32_t num_outputs;
+} AxcIoBuffers;
+
+int32_t axc_step_day_phase_batch(const ShardVramPtrs* vram, uint32_t padded_n,
+                                 uint32_t total_axons, uint32_t sync_batch_ticks,
+                                 const AxcIoBuffers* io, const uint32_t* h_input_bitmask,
+                                 const uint32_t* h_incoming_spikes,
+                                 const uint32_t* h_spike_counts, uint32_t virtual_offset,
+                                 uint32_t num_virtual_axons, const uint32_t* mapped_soma_ids_device,
+                                 uint32_t v_seg, int16_t dopamine, uint32_t tick_base,
+                                 uint8_t* h_output_history, void* stream);
+
+/* Instrumented ticks for measurement: runs `ticks` ticks as cu_step_day_phase
+ * does (tick = tick0 + k, bitmask row k of the device array d_input_bitmask),
+ * with CUDA events recorded on `stream` around each stage.  Adds the stage
+ * times in milliseconds to out_ms[5] (network ids, axons, update, push,
+ * GSOP) and writes the ticks' totals of evaluated slots, hits, spikes and
+ * GSOP slots to out_counts[4].  Synchronous. */
+int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons,
+                          uint32_t v_seg, uint32_t tick0, uint32_t ticks,
+                          const uint32_t* d_input_bitmask, uint32_t words_per_tick,
+                          uint32_t virtual_offset, uint32_t num_virtual, int16_t dopamine,
+                          void* stream, float* out_ms, uint64_t* out_counts);
+
+/* Per-tick counters accumulated by the device since the last reset:
+ *  [0] ticks, [1] evaluated slots (non-refractory neurons, up to first empty),
+ *  [2] delivered hits, [3] GLIF+heartbeat spikes, [4] GSOP slots updated. */
+int32_t axc_shard_counters(const ShardVramPtrs* vram, uint32_t reset, uint64_t out[8]);
+
+/* ---- Synthetic brain generator (host) ---------------------------------- */
+/* Neurons fill a dim_x*dim_y*dim_z voxel grid (x fastest, one per voxel);
+ * neuron n owns axon n; input v owns virtual axon padded_n + v and sits on a
+ * seeded distinct voxel.  Each neuron binds `slots` distinct presynaptic
+ * axons (no self-synapse) drawn with probability proportional to
+ * exp(-dist/lambda) over all neurons and inputs within `radius` voxels.  The
+ * segment is 1 + floor(dist)/2 (two voxels per segment).  Weights are
+ * uniform in [w_min, w_max], negative for inhibitory presynaptic neurons.  */
+typedef struct AxcBrainSpec {
+  uint32_t dim_x, dim_y, dim_z;
+  uint32_t slots;              /* used dendrite slots per neuron (<= 128) */
+  uint32_t num_inputs;         /* virtual input axons */
+  uint32_t inhibitory_permille;/* 200 = 20% inhibitory */
+  uint32_t radius;             /* sampling support, voxels */
+  uint32_t lambda_voxels;      /* exp(-dist/lambda) */
+  int32_t w_min, w_max;        /* |weight| range */
+  uint64_t seed;
+} AxcBrainSpec;
+
+typedef struct AxcBrainLayout {
+  uint32_t num_neurons;
+  uint32_t padded_n;
+  uint32_t total_axons;
+  uint32_t virtual_offset;
+  uint64_t state_bytes;
+  uint64_t axons_bytes;
+} AxcBrainLayout;
+
+int32_t axc_brain_layout(const AxcBrainSpec* spec, AxcBrainLayout* out);
+/* Writes the .state blob (layout.state_bytes) and .axons blob (all sentinel). */
+int32_t axc_brain_generate(const AxcBrainSpec* spec, void* state_blob, void* axons_blob,
+                           int32_t n_threads);
+/* Seeded Bernoulli input bitmask, [ticks][ceil(num_inputs/32)] words; input v
+ * fires at tick t when hash(seed, t, v) < p_q32[t % period] (p in Q0.32). */
+int32_t axc_input_bitmask(uint64_t seed, uint32_t tick0, uint32_t ticks, uint32_t num_inputs,
+                          const uint32_t* p_q32, uint32_t period, uint32_t* out_words);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* AXICOR_DAY_H */
