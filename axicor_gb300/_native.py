@@ -147,6 +147,8 @@ SIGNATURES: dict[str, tuple] = {
     "axc_step_day_phase_batch": (I32, [PV, U32, U32, U32, C.POINTER(AxcIoBuffers), P, P, P, U32, U32, P, U32,
                                        I16, U32, P, P]),
     "axc_shard_counters": (I32, [PV, U32, C.POINTER(C.c_uint64)]),
+    "axc_profile_ticks": (I32, [PV, U32, U32, U32, U32, U32, P, U32, U32, U32, I16, P, C.POINTER(C.c_float),
+                                C.POINTER(C.c_uint64)]),
     "axc_brain_layout": (I32, [C.POINTER(AxcBrainSpec), C.POINTER(AxcBrainLayout)]),
     "axc_brain_generate": (I32, [C.POINTER(AxcBrainSpec), P, P, I32]),
     "axc_input_bitmask": (I32, [C.c_uint64, U32, U32, U32, P, U32, P]),
