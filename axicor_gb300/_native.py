@@ -149,6 +149,7 @@ SIGNATURES: dict[str, tuple] = {
     "axc_shard_counters": (I32, [PV, U32, C.POINTER(C.c_uint64)]),
     "axc_profile_ticks": (I32, [PV, U32, U32, U32, U32, U32, P, U32, U32, U32, I16, P, C.POINTER(C.c_float),
                                 C.POINTER(C.c_uint64)]),
+    "axc_extract_outgoing_spikes_noalloc": (I32, [P, P, P, U32, U32, U32, P, P, P]),
     "axc_brain_layout": (I32, [C.POINTER(AxcBrainSpec), C.POINTER(AxcBrainLayout)]),
     "axc_brain_generate": (I32, [C.POINTER(AxcBrainSpec), P, P, I32]),
     "axc_input_bitmask": (I32, [C.c_uint64, U32, U32, U32, P, U32, P]),

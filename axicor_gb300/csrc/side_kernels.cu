@@ -4,6 +4,9 @@
 // that ffi.rs:193-233 declares.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
+
+#include <mutex>
 
 #include "engine.h"
 
@@ -257,6 +260,41 @@ __global__ void __launch_bounds__(256) k_legacy_readout(const uint8_t* __restric
   out[(size_t)tick * channels + tid] = id < N ? (flags[id] & 0x01) : 0;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch of the allocation-free spike extraction: the per-block event totals
+// (then offsets) of one call, for up to AXC_NOALLOC_MAX_BOUNDARY_AXONS entries.
+// Every GPU that loads this library holds these 16 KiB until the process
+// exits.  Every call overwrites the totals of the blocks it uses before it
+// reads them, so nothing has to start at zero; two calls that overlap on the
+// GPU (for example on two streams) use the same array and race.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoAllocBlocks = AXC_NOALLOC_MAX_BOUNDARY_AXONS / kExtBlock;
+static_assert(AXC_NOALLOC_MAX_BOUNDARY_AXONS % kExtBlock == 0, "whole blocks");
+static __device__ __align__(256) uint32_t g_noalloc_block_totals[kNoAllocBlocks];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_block_totals on the current device.  Host code
+// cannot pass the symbol itself: on the host it names a shadow variable, not
+// device memory.  Looked up once per device, with that device current.
+cudaError_t noalloc_scratch(uint32_t** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_block_totals);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = static_cast<uint32_t*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
 ShardVramPtrs from_legacy(const VramState& s) {
   ShardVramPtrs v;
   v.soma_voltage = s.voltage;
@@ -306,6 +344,38 @@ void launch_extract_outgoing_spikes(const BurstHeads8* axon_heads, const uint32_
   k_ext_write<<<nb, kExtBlock, 0, stream>>>(axon_heads, src_indices, dst_ghost_ids, count, sync_batch_ticks, v_seg,
                                             tmp, static_cast<SpikeEvent*>(out_events));
   cudaFreeAsync(tmp, stream);
+}
+
+// The same extraction as launch_extract_outgoing_spikes, for callers that must
+// not allocate device memory: its scratch is the file-scope array above, so the
+// call launches kernels and nothing else (no cudaMalloc, cudaFree or pool
+// allocation).  The first call on a device looks up the array's address.
+int32_t axc_extract_outgoing_spikes_noalloc(const BurstHeads8* axon_heads, const uint32_t* src_indices,
+                                            const uint32_t* dst_ghost_ids, uint32_t count, uint32_t sync_batch_ticks,
+                                            uint32_t v_seg, void* out_events, uint32_t* out_count, void* stream_v) {
+  if (count > AXC_NOALLOC_MAX_BOUNDARY_AXONS) {
+    fprintf(stderr,
+            "[axc_extract_outgoing_spikes_noalloc] %u boundary axons exceed the fixed scratch limit of %u; "
+            "use launch_extract_outgoing_spikes or split the call\n",
+            count, (unsigned)AXC_NOALLOC_MAX_BOUNDARY_AXONS);
+    return (int32_t)cudaErrorInvalidValue;
+  }
+  if (!out_count || (count > 0 && (!axon_heads || !src_indices || !dst_ghost_ids || !out_events)))
+    return (int32_t)cudaErrorInvalidValue;
+  uint32_t* totals = nullptr;
+  cudaError_t e = noalloc_scratch(&totals);
+  if (e != cudaSuccess) return (int32_t)e;
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  if (count == 0 || v_seg == 0) {
+    k_scan_totals<<<1, 1024, 0, stream>>>(totals, 0, out_count, 0);   // writes *out_count = 0
+    return (int32_t)cudaGetLastError();
+  }
+  const uint32_t nb = (count + kExtBlock - 1) / kExtBlock;
+  k_ext_count<<<nb, kExtBlock, 0, stream>>>(axon_heads, src_indices, count, sync_batch_ticks, v_seg, totals);
+  k_scan_totals<<<1, 1024, 0, stream>>>(totals, nb, out_count, 0);
+  k_ext_write<<<nb, kExtBlock, 0, stream>>>(axon_heads, src_indices, dst_ghost_ids, count, sync_batch_ticks, v_seg,
+                                            totals, static_cast<SpikeEvent*>(out_events));
+  return (int32_t)cudaGetLastError();
 }
 
 // bindings.cu:780-782 is a no-op in the reference; so is this.

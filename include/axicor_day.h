@@ -282,6 +282,28 @@ int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
  *  [2] delivered hits, [3] GLIF+heartbeat spikes, [4] GSOP slots updated. */
 int32_t axc_shard_counters(const ShardVramPtrs* vram, uint32_t reset, uint64_t out[8]);
 
+/* Allocation-free outgoing-spike extraction.  No counterpart in the
+ * reference: it is launch_extract_outgoing_spikes (same arguments, same
+ * events in the same order) for callers that may not allocate device memory
+ * at that point — for example a node loop that extracts spikes after every
+ * batch while other shards keep their streams busy (cudaMalloc/cudaFree can
+ * synchronize the whole device), or a deployment that reserves all device
+ * memory at boot and forbids allocation in the per-batch loop.
+ * Its scratch is a fixed 16 KiB device array inside this library, held by
+ * every GPU that loads the library until the process exits; it covers at most
+ * AXC_NOALLOC_MAX_BOUNDARY_AXONS boundary axons per call, and a larger
+ * `count` returns cudaErrorInvalidValue without launching anything.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (two streams, two threads) race and must be
+ * serialised by the caller.  Returns 0 or a cudaError_t. */
+#define AXC_NOALLOC_MAX_BOUNDARY_AXONS (1u << 20)
+int32_t axc_extract_outgoing_spikes_noalloc(const BurstHeads8* axon_heads,
+                                            const uint32_t* src_indices,
+                                            const uint32_t* dst_ghost_ids, uint32_t count,
+                                            uint32_t sync_batch_ticks, uint32_t v_seg,
+                                            void* out_events, uint32_t* out_count, void* stream);
+
 /* ---- Synthetic brain generator (host) ---------------------------------- */
 /* Neurons fill a dim_x*dim_y*dim_z voxel grid (x fastest, one per voxel);
  * neuron n owns axon n; input v owns virtual axon padded_n + v and sits on a
