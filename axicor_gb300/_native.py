@@ -147,8 +147,10 @@ SIGNATURES: dict[str, tuple] = {
     "axc_step_day_phase_batch": (I32, [PV, U32, U32, U32, C.POINTER(AxcIoBuffers), P, P, P, U32, U32, P, U32,
                                        I16, U32, P, P]),
     "axc_shard_counters": (I32, [PV, U32, C.POINTER(C.c_uint64)]),
-    "axc_profile_ticks": (I32, [PV, U32, U32, U32, U32, U32, P, U32, U32, U32, I16, P, C.POINTER(C.c_float),
+    "axc_profile_ticks": (I32, [PV, U32, U32, U32, U32, U32, P, U32, U32, U32, I16, I32, P, C.POINTER(C.c_float),
                                 C.POINTER(C.c_uint64)]),
+    "axc_batch_engine_mode": (I32, [I32]),
+    "axc_row_engine_fix_capacity": (U32, [U32]),
     "axc_extract_outgoing_spikes_noalloc": (I32, [P, P, P, U32, U32, U32, P, P, P]),
     "axc_brain_layout": (I32, [C.POINTER(AxcBrainSpec), C.POINTER(AxcBrainLayout)]),
     "axc_brain_generate": (I32, [C.POINTER(AxcBrainSpec), P, P, I32]),

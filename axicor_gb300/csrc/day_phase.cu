@@ -110,6 +110,7 @@ __device__ __forceinline__ void block_count(unsigned long long a, unsigned long 
   __shared__ unsigned long long red[3][32];
   a = warp_sum(a); b = warp_sum(b); c = warp_sum(c);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();  // a previous call's reader is done with red[]
   if (lane == 0) { red[0][w] = a; red[1][w] = b; red[2][w] = c; }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(256) k_update(ShardVramPtrs P, uint32_t N, uin
   const uint32_t tick = batch ? ctl->tick_base + k : tick_arg;
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   int spike = 0;
-  uint32_t ev = 0, hits = 0, err = 0;
+  uint32_t ev = 0, hits = 0, err = 0, nev = 0;
   if (n < N) {
     const uint8_t flags = P.soma_flags[n];
     const uint8_t timer = P.timers[n];
@@ -206,6 +207,7 @@ __global__ void __launch_bounds__(256) k_update(ShardVramPtrs P, uint32_t N, uin
       P.timers[n] = (uint8_t)(timer - 1);
       P.soma_flags[n] = ftype;
     } else {
+      nev = 1;
       const VariantParameters& p = lut[flags >> 4];
       const uint32_t prop = p.signal_propagation_length;
       const bool mask_exact = prop == s_pmax;
@@ -295,6 +297,7 @@ __global__ void __launch_bounds__(256) k_update(ShardVramPtrs P, uint32_t N, uin
   const uint32_t err_any = __reduce_or_sync(kFull, err);
   if (err_any && (threadIdx.x & 31) == 0) atomicOr(&ctl->err, err_any);
   block_count(ev, hits, (unsigned long long)spike, &ctl->ctr[1]);
+  block_count(0, nev, 0, &ctl->ctr[4]);
 }
 
 // ---------------------------------------------------------------------------
@@ -310,6 +313,11 @@ __global__ void __launch_bounds__(256) k_push(BurstHeads8* __restrict__ heads, c
   const uint32_t cnt = ctl->spike_count;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid == 0) {  // the row engine's per-tick lists start empty next tick
+    ctl->eval_count = 0;
+    ctl->fix_count = 0;
+    ctl->fix_overflow = 0;
+  }
   for (uint32_t i = tid; i < cnt; i += stride) {
     const uint32_t ax = s2a[spikers[i]];
     if (ax >= A) continue;
@@ -512,6 +520,11 @@ __global__ void __launch_bounds__(kListBlock) k_list_write(const uint8_t* __rest
 }
 
 }  // namespace
+}  // namespace axc
+
+#include "row_engine.cuh"
+
+namespace axc {
 
 int sm_count() {
   static int cached = 0;
@@ -548,6 +561,7 @@ cudaError_t launch_tick(const ShardVramPtrs& v, ShardScratch& s, const TickArgs&
     k_incoming<<<sms, 256, 0, stream>>>(a.incoming_spikes, a.num_incoming, batch_counts, a.k,
                                         a.max_incoming, A, s.incoming);
   if (ev) cudaEventRecord(ev[1], stream);
+  if (a.rows) return launch_tick_rows(v, s, a, stream, ev, have_incoming);
   const uint32_t* bitmask = (a.num_virtual > 0) ? a.input_bitmask : nullptr;
   uint32_t raise = 0;
   if (bitmask && ((uint64_t)a.virtual_offset + a.num_virtual > A)) raise |= AXC_ERR_VIRTUAL_RANGE;

@@ -14,8 +14,25 @@ struct ShardCtl {
   uint32_t err;           // AXC_ERR_* bits, sticky until read with clear
   uint32_t tick_base;     // batch mode: global tick of tick 0 of the batch
   int32_t dopamine;       // batch mode: dopamine of the batch
-  uint32_t pad[4];
+  uint32_t eval_count;    // row engine: non-refractory neurons listed this tick
+  uint32_t fix_count;     // row engine: GSOP slots deferred to the fix-up stage
+  uint32_t fix_overflow;  // row engine: the fix-up list overflowed, rescan the spikers
+  uint32_t pad;
   unsigned long long ctr[8];  // statistics, see axc_shard_counters
+};
+
+// Neuron-major copy of the dendrites used by the batch engine for the length
+// of one batch (row_engine.cuh).
+struct RowCache {
+  uint32_t N = 0, A = 0;
+  void* base = nullptr;
+  uint32_t* rt = nullptr;   // [N][128] targets, neuron-major
+  int16_t* rw = nullptr;    // [N][128] weights, neuron-major
+  uint8_t* cnt = nullptr;   // [N] slots before the first empty target
+  uint2* mask2 = nullptr;   // [A] split segment-hit masks (heads 0..6 | head 7)
+  uint32_t* mult = nullptr; // [A] number of somas that own the axon
+  uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
+  uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
 };
 
 // Per-shard scratch owned by the engine, next to the reference-visible
@@ -33,7 +50,16 @@ struct ShardScratch {
   uint32_t batch_cap = 0;
   uint32_t* h_counts_pinned = nullptr;  // pinned staging for batch_counts / tick_base
   void* graph_cache = nullptr;          // batch engine graphs (batch_engine.cu)
+  RowCache* rows = nullptr;             // batch engine neuron-major dendrites
 };
+
+constexpr uint32_t kFixCap = 1u << 22;  // deferred GSOP slots per tick before the rescan path
+
+// Row engine (row_engine.cuh, compiled in day_phase.cu).
+cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A);
+void rows_free(ShardScratch& s);
+cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream);
+cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream);
 
 // Registry keyed by the axon_heads pointer.  Created by cu_allocate_shard;
 // created lazily (and sized) for shards whose memory the caller allocated.
@@ -58,6 +84,8 @@ struct TickArgs {
   int16_t dopamine;
   bool batch;                 // read tick/dopamine/count from the device control block
   uint32_t k;                 // tick index inside the batch
+  bool rows;                  // use the neuron-major row engine (batch mode only)
+  uint32_t fix_cap;           // row engine: deferred-GSOP list capacity (<= kFixCap)
 };
 
 // ev (optional): 6 events recorded around the stages (incoming, axons,

@@ -1,0 +1,649 @@
+// row_engine.cuh — the batch engine's neuron-major tick (compiled as part of
+// day_phase.cu: it uses that translation unit's __constant__ LUT and helpers).
+//
+// Why: in the reference layout dendrite slot i of all neurons is one row
+// ([slot][neuron], memory.rs:71-86), so a 32-byte sector holds 8 neurons'
+// targets.  In steady state only the non-refractory quarter of the neurons is
+// evaluated each tick, yet nearly every sector is fetched, and GSOP re-reads
+// the spikers' slots with one sector per slot.  For the length of one batch the
+// engine keeps a neuron-major copy ([neuron][128]) of targets and weights:
+//
+//   batch start  k_rows_build      columnar -> rows, first-empty count per neuron
+//                k_rows_mult       somas per axon (soma_to_axon multiplicity)
+//   per tick     k_rows_prologue   axon pushes + propagation + split masks,
+//                                  refractory countdown, list of evaluated neurons
+//                k_rows_update     8 lanes per evaluated neuron: gather/sum, GLIF,
+//                                  and GSOP in the same pass on the rows in registers
+//                k_rows_fixup      the GSOP slots whose result depends on same-tick pushes
+//                k_push            soma pushes, readout (shared with the columnar path)
+//   batch end    k_rows_writeback  weights rows -> columnar (slots before the first empty)
+//
+// GSOP in the update pass.  GSOP must see the heads after this tick's soma
+// pushes (physics.cu:281-373 runs after the update kernel), which are not all
+// known while neurons are still being updated.  A push inserts a 0 head and
+// drops h7, so for an axon owned by one soma the result can only change when
+// segment 0 is involved or h7 is the only head in the tail.  The axon stage
+// writes two masks per axon — hits of heads 0..6 and hits of head 7 — so the
+// update pass knows, per slot, the "no push" and "one push" outcomes.  When
+// they agree the weight is updated at once; otherwise the slot is left
+// untouched and listed, and k_rows_fixup applies it with the actual push count
+// (and from the original weight).  Axons owned by two or more somas, variants
+// whose length differs from the LUT maximum or exceeds 16 (where the cooling
+// shift can be non-zero) and segments >= 31 take the exact general path.
+
+namespace axc {
+namespace {
+
+constexpr uint32_t kRowStride = AXC_MAX_DENDRITES;   // slots per neuron row
+constexpr uint32_t kInf = 0xFFFFFFFFu;
+
+// physics.cu:322-371 for one slot given the minimum in-tail distance md.
+__device__ __forceinline__ int16_t gsop_weight(int16_t w16, uint32_t md, const VariantParameters& p, int32_t bm,
+                                               int32_t raw_pot, int32_t final_dep) {
+  const bool active = md != kInf;
+  const int32_t sign = w16 >= 0 ? 1 : -1;
+  int32_t abs_w = (int32_t)w16;
+  if (abs_w < 0) abs_w = -abs_w;
+  uint32_t rank = (uint32_t)abs_w >> 11;
+  if (rank > 15) rank = 15;
+  const int32_t inertia = p.inertia_curve[rank];
+  const int32_t delta_pot = wmul(wmul(raw_pot, inertia), bm) >> 7;
+  const int32_t delta_dep = wmul(wmul(final_dep, inertia), bm) >> 7;
+  const uint32_t cs = active ? (md >> 4) : 0u;
+  int32_t delta = active ? (delta_pot >> cs) : wsub(0, delta_dep);
+  delta = wmul(delta, 128) >> (7u + cs);
+  int32_t new_abs = wadd(abs_w, delta);
+  new_abs = new_abs & ~(new_abs >> 31);
+  if (new_abs > 32767) new_abs = 32767;
+  return (int16_t)wmul(new_abs, sign);
+}
+
+__device__ __forceinline__ uint32_t md_of(const uint32_t h[8], uint32_t s, uint32_t len) {
+  uint32_t md = kInf;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const uint32_t d = h[q] - s;
+    md = min(md, d < len ? d : kInf);
+  }
+  return md;
+}
+
+// Minimum distances with no push and with one push (0, h0..h6).
+__device__ __forceinline__ void md_pair(const BurstHeads8* heads, uint32_t a, uint32_t s, uint32_t len,
+                                        uint32_t* md0, uint32_t* md1) {
+  uint32_t h[8];
+  load_heads(heads, a, h);
+  uint32_t m06 = kInf;
+#pragma unroll
+  for (int q = 0; q < 7; q++) {
+    const uint32_t d = h[q] - s;
+    m06 = min(m06, d < len ? d : kInf);
+  }
+  const uint32_t d7 = h[7] - s;
+  *md0 = min(m06, d7 < len ? d7 : kInf);
+  const uint32_t dz = 0u - s;
+  *md1 = min(m06, dz < len ? dz : kInf);
+}
+
+// Per-neuron GSOP constants (physics.cu:290-345).
+struct GsopConsts {
+  int32_t bm, raw_pot, final_dep;
+};
+
+__device__ __forceinline__ GsopConsts gsop_consts(uint8_t flags, const VariantParameters& p, int32_t dopamine) {
+  GsopConsts g;
+  const uint32_t burst = (flags >> 1) & 0x07;
+  g.bm = burst > 0 ? (int32_t)burst : 1;
+  const int32_t pot_mod = wmul(dopamine, (int32_t)p.d1_affinity) >> 7;
+  const int32_t dep_mod = wmul(dopamine, (int32_t)p.d2_affinity) >> 7;
+  g.raw_pot = wadd((int32_t)p.gsop_potentiation, pot_mod);
+  const int32_t raw_dep = wsub((int32_t)p.gsop_depression, dep_mod);
+  g.final_dep = raw_dep & ~(raw_dep >> 31);
+  return g;
+}
+
+// Split segment-hit masks of one axon's (propagated) heads for length P:
+// x: bits 0..30 = segments hit by heads 0..6, bit 31 = some head (0..7) may hit
+//    a segment >= 31;  y: bits 0..30 = segments hit by head 7, bit 31 = the axon
+//    is owned by two or more somas.  An axon owned by no soma cannot be pushed
+//    between update and GSOP, so its head-7 hits are folded into x.
+__device__ __forceinline__ uint2 split_masks(const uint32_t h[8], uint32_t P, uint32_t mult) {
+  uint32_t x = 0, y = 0;
+  if (P != 0) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const uint32_t v = h[k];
+      if (v < 255u + P) {
+        const uint32_t lo = (v + 1u > P) ? v + 1u - P : 0u;
+        uint32_t bits = 0;
+        if (lo <= 30u) {
+          const uint32_t top = min(v, 30u);
+          bits = ((2u << top) - 1u) & ~((1u << lo) - 1u);
+        }
+        if (k < 7) x |= bits; else y |= bits;
+        if (v >= 31u) x |= 0x80000000u;
+      }
+    }
+  }
+  if (mult == 0) { x |= y; y = 0; }
+  if (mult >= 2) y |= 0x80000000u;
+  return make_uint2(x, y);
+}
+
+// True when the update pass may apply GSOP to this slot on the spot.
+// fast: hit/no-hit decides (variant length == LUT max <= 16, segment < 31,
+// axon not multiply owned) and the one-push outcome equals the no-push one.
+__device__ __forceinline__ bool fast_class(uint32_t s, uint2 m, bool gsop_fast) {
+  return gsop_fast && s < 31u && !(m.y >> 31);
+}
+
+__device__ __forceinline__ bool fast_sensitive(uint32_t s, uint2 m) {
+  const bool a0 = ((m.x | m.y) >> s) & 1u;
+  const bool a1 = (s == 0u) || ((m.x >> s) & 1u);
+  return a0 != a1;
+}
+
+// ---------------------------------------------------------------------------
+// batch start: columnar -> neuron-major, first-empty counts.
+// 32 neurons per 256-thread block; rows are read 8 at a time until every
+// neuron of the tile has met its first empty target.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__ targets,
+                                                    const int16_t* __restrict__ weights, uint32_t N,
+                                                    uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
+                                                    uint8_t* __restrict__ cnt) {
+  __shared__ uint32_t s_t[AXC_MAX_DENDRITES][33];
+  __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
+  __shared__ uint32_t s_cnt[32];
+  const uint32_t n0 = blockIdx.x * 32;
+  const uint32_t col = threadIdx.x & 31, r0 = threadIdx.x >> 5;
+  if (threadIdx.x < 32) s_cnt[threadIdx.x] = AXC_MAX_DENDRITES;
+  __syncthreads();
+  for (uint32_t ch = 0; ch < AXC_MAX_DENDRITES / 8; ch++) {
+    const uint32_t r = ch * 8 + r0, n = n0 + col;
+    uint32_t t = 0;
+    int16_t w = 0;
+    if (n < N) {
+      t = __ldcs(targets + (size_t)r * N + n);
+      w = __ldcs(weights + (size_t)r * N + n);
+    }
+    s_t[r][col] = t;
+    s_w[r][col] = w;
+    if (t == 0) atomicMin(&s_cnt[col], r);
+    __syncthreads();
+    const int mine = threadIdx.x < 32 ? (s_cnt[threadIdx.x] < (ch + 1) * 8) : 1;
+    if (__syncthreads_and(mine)) break;
+  }
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t j = warp; j < 32; j += 8) {
+    const uint32_t n = n0 + j;
+    if (n >= N) continue;
+    const uint32_t c = s_cnt[j];
+    for (uint32_t q = lane; q < c; q += 32) {
+      rt[(size_t)n * kRowStride + q] = s_t[q][j];
+      rw[(size_t)n * kRowStride + q] = s_w[q][j];
+    }
+    if (lane == 0) cnt[n] = (uint8_t)min(c, 255u);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ s2a, uint32_t N, uint32_t A,
+                                                   uint32_t* __restrict__ mult) {
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const uint32_t a = s2a[n];
+  if (a < A) atomicAdd(&mult[a], 1u);
+}
+
+// batch end: weights rows -> columnar for slots before the first empty target.
+__global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ weights, uint32_t N,
+                                                        const int16_t* __restrict__ rw,
+                                                        const uint8_t* __restrict__ cnt) {
+  __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
+  __shared__ uint32_t s_c[32];
+  const uint32_t n0 = blockIdx.x * 32;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t j = warp; j < 32; j += 8) {
+    const uint32_t n = n0 + j;
+    const uint32_t c = n < N ? cnt[n] : 0u;
+    if (lane == 0) s_c[j] = c;
+    for (uint32_t q = lane; q < c; q += 32) s_w[q][j] = rw[(size_t)n * kRowStride + q];
+  }
+  __syncthreads();
+  uint32_t cmax = 0;
+  for (int j = 0; j < 32; j++) cmax = max(cmax, s_c[j]);
+  const uint32_t c_mine = s_c[lane];
+  for (uint32_t r = warp; r < cmax; r += 8)
+    if (r < c_mine) weights[(size_t)r * N + n0 + lane] = s_w[r][lane];
+}
+
+// ---------------------------------------------------------------------------
+// per tick 1/4: axons (inject, network pushes, propagate, split masks) and
+// somas (refractory countdown, list of neurons to evaluate).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__ heads, uint32_t A, uint32_t v_seg,
+                                                       const uint32_t* __restrict__ bitmask, uint32_t voff,
+                                                       uint32_t nv, uint32_t* __restrict__ incoming,
+                                                       const uint32_t* __restrict__ batch_counts, uint32_t k,
+                                                       uint2* __restrict__ mask2, const uint32_t* __restrict__ mult,
+                                                       uint8_t* __restrict__ flags, uint8_t* __restrict__ timers,
+                                                       uint32_t N, uint32_t* __restrict__ eval,
+                                                       ShardCtl* __restrict__ ctl, uint32_t raise_err) {
+  __shared__ uint32_t s_pmax;
+  __shared__ int s_inc;
+  if (threadIdx.x == 0) {
+    s_pmax = lut_pmax();
+    s_inc = batch_counts && batch_counts[k] > 0;
+    if (blockIdx.x == 0) {
+      ctl->spike_count = 0;
+      ctl->ctr[0] += 1;
+      if (raise_err) atomicOr(&ctl->err, raise_err);
+    }
+  }
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A) {
+    uint4* p = reinterpret_cast<uint4*>(heads + i);
+    const uint4 x = p[0], y = p[1];
+    uint32_t h[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+    uint32_t npush = 0;
+    if (bitmask) {
+      const uint32_t v = i - voff;
+      if (v < nv) npush += (__ldg(bitmask + (v >> 5)) >> (v & 31u)) & 1u;
+    }
+    if (s_inc) {
+      const uint32_t c = incoming[i];
+      if (c) { npush += c; incoming[i] = 0; }
+    }
+    push_n(h, npush);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (h[j] != AXC_AXON_SENTINEL) h[j] += v_seg;
+    p[0] = make_uint4(h[0], h[1], h[2], h[3]);
+    p[1] = make_uint4(h[4], h[5], h[6], h[7]);
+    mask2[i] = split_masks(h, s_pmax, mult[i]);
+  }
+  bool ev = false;
+  if (i < N) {
+    const uint8_t t = timers[i];
+    if (t > 0) {                                  // physics.cu:168-174 after the burst reset
+      timers[i] = (uint8_t)(t - 1);
+      flags[i] = flags[i] & 0xF0;
+    } else {
+      ev = true;
+    }
+  }
+  const uint32_t ballot = __ballot_sync(kFull, ev);
+  if (ballot) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&ctl->eval_count, (uint32_t)__popc(ballot));
+    base = __shfl_sync(kFull, base, leader);
+    if (ev) eval[base + __popc(ballot & ((1u << lane) - 1u))] = i;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per tick 2/4: 8 lanes per evaluated neuron, lane g holds slots
+// 32j + 4g .. 32j + 4g + 3 (j = 0..3) of the neuron's row in registers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t word_of(const uint4& v, int i) {
+  return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ int16_t half_of(const uint2& v, int i) {
+  const uint32_t w = (i < 2) ? v.x : v.y;
+  return (int16_t)((i & 1) ? (w >> 16) : (w & 0xFFFFu));
+}
+__device__ __forceinline__ void set_half(uint2& v, int i, int16_t x) {
+  uint32_t& w = (i < 2) ? v.x : v.y;
+  w = (i & 1) ? ((w & 0x0000FFFFu) | ((uint32_t)(uint16_t)x << 16)) : ((w & 0xFFFF0000u) | (uint16_t)x);
+}
+
+__global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A,
+                                                        const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
+                                                        const uint8_t* __restrict__ cnt,
+                                                        const uint2* __restrict__ mask2,
+                                                        const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend,
+                                                        uint32_t* __restrict__ spikers, uint32_t* __restrict__ fix,
+                                                        ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap) {
+  __shared__ VariantParameters lut[16];
+  __shared__ uint32_t s_pmax;
+  lut_to_smem(lut);
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
+  __syncthreads();
+  const uint32_t tick = ctl->tick_base + k;
+  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
+  const uint32_t ecount = ctl->eval_count;
+  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
+  for (uint32_t base = wid * 4; base < ecount; base += nwarps * 4) {
+    const uint32_t idx = base + grp;
+    const bool valid = idx < ecount;
+    const uint32_t n = valid ? eval[idx] : 0u;
+    const uint8_t flags = valid ? P.soma_flags[n] : 0;
+    const uint32_t c = valid ? cnt[n] : 0u;
+    const VariantParameters& p = lut[flags >> 4];
+    const uint32_t prop = p.signal_propagation_length;
+    const bool exact = prop == s_pmax;
+    const bool gfast = exact && prop <= 16u;
+    const uint32_t* trow = rt + (size_t)n * kRowStride + 4u * g8;
+    const int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
+    // all four chunks of the row in flight at once
+    uint4 T[4];
+    uint2 W[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (32u * j + 4u * g8 < c) {
+        T[j] = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
+        W[j] = *reinterpret_cast<const uint2*>(wrow + 32 * j);
+      } else {
+        T[j] = make_uint4(0, 0, 0, 0);
+        W[j] = make_uint2(0, 0);
+      }
+    }
+    int32_t i_in = 0;
+    uint32_t hitb = 0, slowb = 0, badb = 0;   // bit 4j+i
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const uint32_t q0 = 32u * j + 4u * g8;
+      uint2 m[4];
+      uint32_t ax[4];
+      bool ok[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        ax[i] = (word_of(T[j], i) & AXC_TARGET_AXON_MASK) - 1u;
+        const bool live = q0 + i < c;
+        ok[i] = live && ax[i] < A;
+        if (live && !ok[i]) badb |= 1u << (4 * j + i);
+        m[i] = ok[i] ? __ldg(mask2 + ax[i]) : make_uint2(0, 0);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        if (!ok[i]) continue;
+        const uint32_t s = word_of(T[j], i) >> AXC_TARGET_SEG_SHIFT;
+        bool hit;
+        if (s < 31u) {
+          hit = ((m[i].x | m[i].y) >> s) & 1u;
+          if (hit && !exact) hit = heads_hit(P.axon_heads, ax[i], s, prop);
+        } else {
+          hit = (m[i].x >> 31) && heads_hit(P.axon_heads, ax[i], s, prop);
+        }
+        if (hit) {
+          i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+          hitb |= 1u << (4 * j + i);
+        }
+        if (!fast_class(s, m[i], gfast) || fast_sensitive(s, m[i])) slowb |= 1u << (4 * j + i);
+      }
+    }
+    if (badb) err |= AXC_ERR_TARGET_RANGE;
+    // sum over the 8 lanes of the neuron
+    i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
+    i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
+    i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
+    ev_slots += (g8 == 0) ? c : 0u;
+    nev += (valid && g8 == 0) ? 1u : 0u;
+    hits += __popc(hitb);
+    // GLIF (physics.cu:209-275); the neuron is not refractory
+    int spike = 0;
+    if (valid) {
+      int32_t thr = P.threshold_offset[n];
+      const int32_t decayed = wsub(thr, (int32_t)p.homeostasis_decay);
+      thr = decayed & ~(decayed >> 31);
+      int32_t leak = p.leak_rate;
+      if (p.adaptive_mode == 1) {
+        leak = wadd(leak, wmul(thr, (int32_t)p.adaptive_leak_gain) >> 8);
+        const int32_t over = wsub(leak, p.adaptive_leak_max);
+        leak = wsub(leak, over & ~(over >> 31));
+      }
+      int32_t v = wadd(P.soma_voltage[n], i_in);
+      const int32_t diff = wsub(v, p.rest_potential);
+      const int32_t sign = (diff > 0) - (diff < 0);
+      int32_t leaked = wsub(wmul(diff, sign), leak);
+      leaked = leaked & ~(leaked >> 31);
+      v = wadd(p.rest_potential, wmul(sign, leaked));
+      const int glif = v >= wadd(p.threshold, thr) ? 1 : 0;
+      const uint32_t period = p.spontaneous_firing_period_ticks;
+      const int hb = (period > 0 && ((tick + n * 104729u) % period) == 0) ? 1 : 0;
+      spike = glif | hb;
+      if (glif) {
+        v = p.rest_potential;
+        thr = wadd(thr, p.homeostasis_penalty);
+      }
+      if (g8 == 0) {
+        P.soma_voltage[n] = v;
+        P.soma_flags[n] = (uint8_t)((flags & 0xF0) | (spike ? 0x05 : 0x00));
+        P.threshold_offset[n] = thr;
+        P.timers[n] = glif ? p.refractory_period : 0;
+        if (spike) {
+          const uint32_t my_axon = P.soma_to_axon[n];
+          if (my_axon != AXC_NO_AXON) {
+            if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
+            else err |= AXC_ERR_SOMA_AXON;
+          }
+        }
+      }
+    }
+    // spiker list (one entry per neuron, from its lane 0)
+    const uint32_t lead = __ballot_sync(kFull, spike && g8 == 0);
+    if (lead) {
+      const int leader = __ffs(lead) - 1;
+      uint32_t b0 = 0;
+      if ((int)lane == leader) b0 = atomicAdd(&ctl->spike_count, (uint32_t)__popc(lead));
+      b0 = __shfl_sync(kFull, b0, leader);
+      if (spike && g8 == 0) spikers[b0 + __popc(lead & ((1u << lane) - 1u))] = n;
+      nspk += (spike && g8 == 0) ? 1u : 0u;
+    }
+    // GSOP on the same rows (physics.cu:281-373); the chunks are reloaded from L1
+    if (spike) {
+      const GsopConsts gc = gsop_consts((uint8_t)((flags & 0xF0) | 0x05), p, dopamine);
+#pragma unroll 1
+      for (int j = 0; j < 4; j++) {
+        const uint32_t q0 = 32u * j + 4u * g8;
+        if (q0 >= c) break;
+        const uint4 tj = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
+        uint2 wj = *reinterpret_cast<const uint2*>(wrow + 32 * j);
+        bool dirty = false;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint32_t b = 1u << (4 * j + i);
+          if (q0 + i >= c || (badb & b)) continue;
+          gdone++;
+          uint32_t md;
+          if (!(slowb & b)) {
+            md = (hitb & b) ? 0u : kInf;
+          } else {
+            const uint32_t t = word_of(tj, i);
+            const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
+            const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+            const uint2 m = __ldg(mask2 + a);
+            uint32_t md1;
+            md_pair(P.axon_heads, a, s, prop, &md, &md1);
+            if ((m.y >> 31) || md != md1) {
+              const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+              if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
+              else ctl->fix_overflow = 1u;
+              continue;
+            }
+          }
+          set_half(wj, i, gsop_weight(half_of(wj, i), md, p, gc.bm, gc.raw_pot, gc.final_dep));
+          dirty = true;
+        }
+        if (dirty) *reinterpret_cast<uint2*>(rw + (size_t)n * kRowStride + q0) = wj;
+      }
+    }
+  }
+  const uint32_t err_any = __reduce_or_sync(kFull, err);
+  if (err_any && lane == 0) atomicOr(&ctl->err, err_any);
+  block_count(ev_slots, hits, nspk, &ctl->ctr[1]);
+  block_count(gdone, nev, 0, &ctl->ctr[4]);
+}
+
+// ---------------------------------------------------------------------------
+// per tick 3/4: deferred GSOP slots, with the actual push count of the axon
+// (pend, before k_push consumes it) and the original weight.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fixup_slot(const ShardVramPtrs& P, const VariantParameters* lut, uint32_t A,
+                                           const uint32_t* rt, int16_t* rw, const uint32_t* pend,
+                                           uint32_t r, int32_t dopamine) {
+  const uint32_t n = r / kRowStride;
+  const uint32_t t = rt[r];
+  const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
+  const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+  const uint8_t flags = P.soma_flags[n];
+  const VariantParameters& p = lut[flags >> 4];
+  uint32_t h[8];
+  load_heads(P.axon_heads, a, h);
+  push_n(h, pend[a]);
+  const uint32_t md = md_of(h, s, p.signal_propagation_length);
+  const GsopConsts gc = gsop_consts(flags, p, dopamine);
+  rw[r] = gsop_weight(rw[r], md, p, gc.bm, gc.raw_pot, gc.final_dep);
+}
+
+__global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N, uint32_t A,
+                                                    const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
+                                                    const uint8_t* __restrict__ cnt,
+                                                    const uint2* __restrict__ mask2, const uint32_t* __restrict__ pend,
+                                                    const uint32_t* __restrict__ spikers,
+                                                    const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl) {
+  const uint32_t nfix = ctl->fix_count;
+  const uint32_t overflow = ctl->fix_overflow;
+  if (nfix == 0 && !overflow) return;
+  __shared__ VariantParameters lut[16];
+  __shared__ uint32_t s_pmax;
+  lut_to_smem(lut);
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
+  __syncthreads();
+  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!overflow) {
+    for (uint32_t i = tid; i < nfix; i += stride) fixup_slot(P, lut, A, rt, rw, pend, fix[i], dopamine);
+    return;
+  }
+  // the list overflowed: rescan every spiker's slots with the update pass's rule
+  const uint32_t nsp = ctl->spike_count;
+  for (uint32_t w = tid; w < nsp * kRowStride; w += stride) {
+    const uint32_t n = spikers[w / kRowStride], q = w % kRowStride;
+    if (q >= cnt[n]) continue;
+    const uint32_t r = n * kRowStride + q;
+    const uint32_t t = rt[r];
+    const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
+    if (a >= A) continue;
+    const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+    const VariantParameters& p = lut[P.soma_flags[n] >> 4];
+    const uint32_t prop = p.signal_propagation_length;
+    const bool gfast = prop == s_pmax && prop <= 16u;
+    const uint2 m = mask2[a];
+    bool defer;
+    if (fast_class(s, m, gfast) && !fast_sensitive(s, m)) {
+      defer = false;
+    } else {
+      uint32_t md0, md1;
+      md_pair(P.axon_heads, a, s, prop, &md0, &md1);
+      defer = (m.y >> 31) || md0 != md1;
+    }
+    if (defer) fixup_slot(P, lut, A, rt, rw, pend, r, dopamine);
+  }
+}
+
+__global__ void k_rows_reset_lists(ShardCtl* ctl) {
+  ctl->eval_count = 0;
+  ctl->fix_count = 0;
+  ctl->fix_overflow = 0;
+}
+
+}  // namespace
+
+cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A) {
+  if (s.rows && s.rows->N >= N && s.rows->A >= A) return cudaSuccess;
+  rows_free(s);
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t off = 0;
+  const size_t o_rt = off; off = al(off + (size_t)N * kRowStride * 4);
+  const size_t o_rw = off; off = al(off + (size_t)N * kRowStride * 2);
+  const size_t o_cnt = off; off = al(off + (size_t)N);
+  const size_t o_m2 = off; off = al(off + (size_t)A * 8);
+  const size_t o_mult = off; off = al(off + (size_t)A * 4);
+  const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
+  const size_t o_fix = off; off = al(off + (size_t)kFixCap * 4);
+  void* base = nullptr;
+  cudaError_t e = cudaMalloc(&base, off);
+  if (e != cudaSuccess) return e;
+  e = cudaMemset(base, 0, off);
+  if (e != cudaSuccess) { cudaFree(base); return e; }
+  RowCache* r = new RowCache();
+  char* b = static_cast<char*>(base);
+  r->N = N;
+  r->A = A;
+  r->base = base;
+  r->rt = reinterpret_cast<uint32_t*>(b + o_rt);
+  r->rw = reinterpret_cast<int16_t*>(b + o_rw);
+  r->cnt = reinterpret_cast<uint8_t*>(b + o_cnt);
+  r->mask2 = reinterpret_cast<uint2*>(b + o_m2);
+  r->mult = reinterpret_cast<uint32_t*>(b + o_mult);
+  r->eval = reinterpret_cast<uint32_t*>(b + o_eval);
+  r->fix = reinterpret_cast<uint32_t*>(b + o_fix);
+  s.rows = r;
+  return cudaSuccess;
+}
+
+void rows_free(ShardScratch& s) {
+  if (!s.rows) return;
+  cudaFree(s.rows->base);
+  delete s.rows;
+  s.rows = nullptr;
+}
+
+cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream) {
+  RowCache& r = *s.rows;
+  k_rows_reset_lists<<<1, 1, 0, stream>>>(s.ctl);
+  cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
+  if (e != cudaSuccess) return e;
+  if (N) {
+    k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult);
+    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt);
+  }
+  return cudaGetLastError();
+}
+
+// One tick of the row engine (batch mode): prologue, update (+GSOP), fix-up, push.
+// ev (optional) gets the stage boundaries 2..5 recorded (GSOP is part of update).
+cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
+                             cudaEvent_t* ev, bool have_incoming) {
+  RowCache& r = *s.rows;
+  const uint32_t N = a.padded_n, A = a.total_axons;
+  const int sms = sm_count();
+  const uint32_t* bitmask = (a.num_virtual > 0) ? a.input_bitmask : nullptr;
+  uint32_t raise = 0;
+  if (bitmask && ((uint64_t)a.virtual_offset + a.num_virtual > A)) raise |= AXC_ERR_VIRTUAL_RANGE;
+  const uint32_t G = max(A, N);
+  if (G)
+    k_rows_prologue<<<(G + 255) / 256, 256, 0, stream>>>(
+        v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
+        have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
+        raise);
+  if (ev) cudaEventRecord(ev[2], stream);
+  k_rows_update<<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, s.spikers, r.fix,
+                                             s.ctl, a.k, min(a.fix_cap, kFixCap));
+  if (ev) cudaEventRecord(ev[3], stream);
+  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, s.spikers, r.fix, s.ctl);
+  const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
+  k_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, s.spikers, s.ctl, v.soma_flags, N,
+                                      a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0);
+  if (ev) {
+    cudaEventRecord(ev[4], stream);
+    cudaEventRecord(ev[5], stream);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream) {
+  RowCache& r = *s.rows;
+  if (N) k_rows_writeback<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_weights, N, r.rw, r.cnt);
+  return cudaGetLastError();
+}
+
+}  // namespace axc

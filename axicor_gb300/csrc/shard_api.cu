@@ -376,46 +376,6 @@ int32_t axc_shard_counters(const ShardVramPtrs* vram, uint32_t reset, uint64_t o
   return (int32_t)e;
 }
 
-int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons, uint32_t v_seg,
-                          uint32_t tick0, uint32_t ticks, const uint32_t* d_input_bitmask, uint32_t words_per_tick,
-                          uint32_t virtual_offset, uint32_t num_virtual, int16_t dopamine, void* stream_v,
-                          float* out_ms, uint64_t* out_counts) {
-  if (!vram || !out_ms || !out_counts) return (int32_t)cudaErrorInvalidValue;
-  cudaError_t e;
-  ShardScratch* s = scratch_for(vram, padded_n, total_axons, &e);
-  if (!s) return (int32_t)e;
-  cudaStream_t st = static_cast<cudaStream_t>(stream_v);
-  cudaEvent_t ev[kTickStages + 1];
-  for (int i = 0; i <= kTickStages; i++) cudaEventCreate(&ev[i]);
-  unsigned long long c0[8], c1[8];
-  e = cudaStreamSynchronize(st);
-  if (e == cudaSuccess) e = cudaMemcpy(c0, s->ctl->ctr, sizeof(c0), cudaMemcpyDeviceToHost);
-  for (int i = 0; i < kTickStages; i++) out_ms[i] = 0.f;
-  for (uint32_t k = 0; k < ticks && e == cudaSuccess; k++) {
-    TickArgs a{};
-    a.padded_n = padded_n;
-    a.total_axons = total_axons;
-    a.v_seg = v_seg;
-    a.tick = tick0 + k;
-    a.input_bitmask = d_input_bitmask ? d_input_bitmask + (size_t)k * words_per_tick : nullptr;
-    a.virtual_offset = virtual_offset;
-    a.num_virtual = a.input_bitmask ? num_virtual : 0;
-    a.dopamine = dopamine;
-    e = launch_tick(*vram, *s, a, st, ev);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[kTickStages]);
-    for (int i = 0; i < kTickStages && e == cudaSuccess; i++) {
-      float ms = 0.f;
-      e = cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
-      out_ms[i] += ms;
-    }
-  }
-  if (e == cudaSuccess) e = cudaMemcpy(c1, s->ctl->ctr, sizeof(c1), cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess)
-    for (int i = 0; i < 4; i++) out_counts[i] = c1[i + 1] - c0[i + 1];
-  for (int i = 0; i <= kTickStages; i++) cudaEventDestroy(ev[i]);
-  return (int32_t)e;
-}
-
 int32_t axc_last_spikes(const ShardVramPtrs* vram, uint32_t* out_count, uint32_t* out_ids, uint32_t capacity,
                         void* stream) {
   if (!vram || !out_count) return (int32_t)cudaErrorInvalidValue;

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--outputs", type=int, default=4096)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--engine", default="rows", choices=["rows", "columnar"],
+                    help="batch kernels: neuron-major row engine (default) or the per-tick columnar kernels")
     return ap.parse_args()
 
 
@@ -146,8 +148,16 @@ def algorithmic_bytes(ticks, evaluated, spikes, gsop_slots, N, A, I, num_outputs
 
 
 def update_kernel_bytes(ticks, evaluated, spikes, N):
-    """Algorithmic bytes of the update kernel: 6 B per evaluated slot, 20 B per neuron, 4 B per spike."""
+    """Algorithmic bytes of the columnar update kernel: 6 B per evaluated slot, 20 B per neuron, 4 B per spike."""
     return 6 * evaluated + ticks * 20 * N + 4 * spikes
+
+
+def rows_update_kernel_bytes(evaluated_slots, gsop_slots, evaluated_neurons, spikes):
+    """Algorithmic bytes of the row engine's update+GSOP kernel: 6 B per evaluated slot (u32 target + i16
+    weight read), 2 B per GSOP slot (weight written), 24 B per evaluated neuron (flags, slot count, list
+    entry, voltage and threshold read; voltage, flags, threshold, timer written), 4 B per spike
+    (soma_to_axon)."""
+    return 6 * evaluated_slots + 2 * gsop_slots + 24 * evaluated_neurons + 4 * spikes
 
 
 def run_gb300(args, dist: Dist) -> dict | None:
@@ -158,6 +168,8 @@ def run_gb300(args, dist: Dist) -> dict | None:
 
     lib = N.lib()
     lib.gpu_set_device(dist.local_rank)
+    engine = 1 if args.engine == "rows" else 0
+    lib.axc_batch_engine_mode(engine)
     w = workload(args.workload)
     B, K, Wm = args.ticks_per_step, args.steps, args.warmup
     lay, state, heads = S.generate_brain(w.spec())
@@ -243,25 +255,33 @@ def run_gb300(args, dist: Dist) -> dict | None:
     # per-kernel CUDA-event timing on the launching stream (same regime, right after)
     prof_ticks = min(50, B)
     out_ms = (C.c_float * 5)()
-    out_cnt = (C.c_uint64 * 4)()
+    out_cnt = (C.c_uint64 * 5)()
     d_prof_bm = S.device_array(bm_all[:prof_ticks * words])
     err = lib.axc_profile_ticks(C.byref(vram.ptrs), lay.padded_n, lay.total_axons, w.v_seg, tick, prof_ticks,
-                                d_prof_bm, words, lay.virtual_offset, w.num_inputs, w.dopamine, eng.stream, out_ms,
-                                out_cnt)
+                                d_prof_bm, words, lay.virtual_offset, w.num_inputs, w.dopamine, engine, eng.stream,
+                                out_ms, out_cnt)
     if err:
         raise RuntimeError(f"axc_profile_ticks failed: {err}")
     stage_ms = list(out_ms)
-    names = ["network_ids", "axons", "update", "push", "gsop"]
+    if engine == 1:
+        names = ["network_ids", "prologue", "update_gsop", "fixup_push", "gsop"]
+        kernels = {"prologue": "k_rows_prologue", "update_gsop": "k_rows_update", "fixup_push": "k_rows_fixup+k_push"}
+    else:
+        names = ["network_ids", "axons", "update", "push", "gsop"]
+        kernels = {"axons": "k_axons", "update": "k_update", "push": "k_push", "gsop": "k_gsop"}
     top = int(np.argmax(stage_ms))
-    ev, hits, spk, gs = (int(x) for x in out_cnt)
-    if names[top] == "update":
+    ev, hits, spk, gs, nev = (int(x) for x in out_cnt)
+    A_ = lay.total_axons
+    if names[top] == "update_gsop":
+        kb = rows_update_kernel_bytes(ev, gs, nev, spk)
+    elif names[top] == "update":
         kb = update_kernel_bytes(prof_ticks, ev, spk, lay.padded_n)
     elif names[top] == "gsop":
         kb = 8 * gs
-    elif names[top] == "axons":
-        kb = prof_ticks * (64 * lay.total_axons + 4 * lay.total_axons)
+    elif names[top] in ("axons", "prologue"):
+        kb = prof_ticks * (64 * A_ + (8 if engine == 1 else 4) * A_ + (4 + 4) * lay.padded_n)
     else:
-        kb = 4 * spk
+        kb = 68 * spk
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = kb / (stage_ms[top] / 1e3) / 1e9
@@ -279,14 +299,16 @@ def run_gb300(args, dist: Dist) -> dict | None:
         "clocks": clk,
         "h2d": B * words * 4,
         "d2h": B * n_out,
-        "launches": K * (4 * B + 2),
-        "roofline": {"bound": "hbm", "kernel": f"k_update" if names[top] == "update" else f"k_{names[top]}",
+        "launches": K * ((4 * B + 5) if engine == 1 else (4 * B + 2)),
+        "roofline": {"bound": "hbm", "kernel": kernels.get(names[top], names[top]),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
         "stage_ms_per_tick": {n: m / prof_ticks for n, m in zip(names, stage_ms)},
         "tick_algorithmic_gbs": tick_bytes / (ms / 1e3) / 1e9,
         "per_tick": {"evaluated_slots": int(ctr[1]) / ticks_timed, "hits": int(ctr[2]) / ticks_timed,
-                     "spikes": int(ctr[3]) / ticks_timed, "gsop_slots": int(ctr[4]) / ticks_timed},
+                     "spikes": int(ctr[3]) / ticks_timed, "gsop_slots": int(ctr[4]) / ticks_timed,
+                     "evaluated_neurons": int(ctr[5]) / ticks_timed},
+        "engine": args.engine,
         "delivered_events_per_s": value_tps * int(ctr[2]) / ticks_timed,
         "lay": lay, "w": w, "vram": vram,
     }
@@ -299,13 +321,13 @@ def run_gb300(args, dist: Dist) -> dict | None:
 def cpu_sample(w, state, heads, lay, tick0, budget_s, threads) -> dict:
     """Times the CPU restatement of the reference kernels on `threads` host threads."""
     import oracle
+    from axicor_gb300 import shard as S
     words = (w.num_inputs + 31) // 32
     t_once = None
     ticks = 0
     t0 = time.perf_counter()
     while True:
-        bm = __import__("axicor_gb300.shard", fromlist=["x"]).input_bitmask(w.seed, tick0 + ticks, 1, w.num_inputs,
-                                                                             w.rate_q32)
+        bm = S.input_bitmask(w.seed, tick0 + ticks, 1, w.num_inputs, w.rate_q32)
         s = time.perf_counter()
         oracle.run_ticks(state, heads, w.lut, lay.padded_n, lay.total_axons, w.v_seg, tick0 + ticks, 1, bm, words,
                          lay.virtual_offset, w.num_inputs, threads=threads)
@@ -395,7 +417,8 @@ def main():
             "delivered_events_per_s": r["delivered_events_per_s"],
             "config": {"workload": args.workload, "neurons": r["neurons"], "synapses": r["synapses"],
                        "ticks_per_step": args.ticks_per_step, "parallelism": "replicas" if dist.world > 1 else "single",
-                       "l2": "inputs larger than L2 (1.37 GB .state per brain)", "gsop": True},
+                       "l2": "inputs larger than L2 (1.37 GB .state per brain)", "gsop": True,
+                       "engine": r["engine"]},
             "e2e": {"value": r["e2e_events_per_s"], "unit": "events/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ticks_per_s": r["e2e_ticks_per_s"]},
             "gpu_launches": r["launches"],

@@ -265,21 +265,36 @@ int32_t axc_step_day_phase_batch(const ShardVramPtrs* vram, uint32_t padded_n,
                                  uint32_t v_seg, int16_t dopamine, uint32_t tick_base,
                                  uint8_t* h_output_history, void* stream);
 
-/* Instrumented ticks for measurement: runs `ticks` ticks as cu_step_day_phase
- * does (tick = tick0 + k, bitmask row k of the device array d_input_bitmask),
- * with CUDA events recorded on `stream` around each stage.  Adds the stage
- * times in milliseconds to out_ms[5] (network ids, axons, update, push,
- * GSOP) and writes the ticks' totals of evaluated slots, hits, spikes and
- * GSOP slots to out_counts[4].  Synchronous. */
+/* Instrumented ticks for measurement: runs `ticks` ticks (tick = tick0 + k,
+ * bitmask row k of the device array d_input_bitmask) without a graph, with
+ * CUDA events recorded on `stream` around each stage.  engine 0: the
+ * per-tick kernels of cu_step_day_phase; engine 1: the batch engine's
+ * neuron-major kernels (the ticks then form one batch, rows built before and
+ * weights written back after).  Sets out_ms[5] to the stage times in
+ * milliseconds (network ids, axons, update, push, GSOP; with engine 1 GSOP is
+ * part of update and "push" includes the GSOP fix-up) and out_counts[5] to
+ * the ticks' totals of evaluated slots, hits, spikes, GSOP slots and
+ * evaluated (non-refractory) neurons.  Synchronous. */
 int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons,
                           uint32_t v_seg, uint32_t tick0, uint32_t ticks,
                           const uint32_t* d_input_bitmask, uint32_t words_per_tick,
                           uint32_t virtual_offset, uint32_t num_virtual, int16_t dopamine,
-                          void* stream, float* out_ms, uint64_t* out_counts);
+                          int32_t engine, void* stream, float* out_ms, uint64_t* out_counts);
+
+/* Selects the kernels of axc_step_day_phase_batch: 1 (default) the
+ * neuron-major batch engine, 0 the per-tick kernels of cu_step_day_phase.
+ * A negative value only queries.  Returns the previous mode. */
+int32_t axc_batch_engine_mode(int32_t mode);
+
+/* Capacity of the batch engine's per-tick list of deferred GSOP slots
+ * (default and maximum 4,194,304); beyond it the fix-up stage rescans every
+ * spiker.  For tests of that path.  Returns the previous capacity. */
+uint32_t axc_row_engine_fix_capacity(uint32_t cap);
 
 /* Per-tick counters accumulated by the device since the last reset:
  *  [0] ticks, [1] evaluated slots (non-refractory neurons, up to first empty),
- *  [2] delivered hits, [3] GLIF+heartbeat spikes, [4] GSOP slots updated. */
+ *  [2] delivered hits, [3] GLIF+heartbeat spikes, [4] GSOP slots updated,
+ *  [5] evaluated (non-refractory) neurons. */
 int32_t axc_shard_counters(const ShardVramPtrs* vram, uint32_t reset, uint64_t out[8]);
 
 /* Allocation-free outgoing-spike extraction.  No counterpart in the
