@@ -313,11 +313,6 @@ __global__ void __launch_bounds__(256) k_push(BurstHeads8* __restrict__ heads, c
   const uint32_t cnt = ctl->spike_count;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid == 0) {  // the row engine's per-tick lists start empty next tick
-    ctl->eval_count = 0;
-    ctl->fix_count = 0;
-    ctl->fix_overflow = 0;
-  }
   for (uint32_t i = tid; i < cnt; i += stride) {
     const uint32_t ax = s2a[spikers[i]];
     if (ax >= A) continue;

@@ -14,10 +14,9 @@ struct ShardCtl {
   uint32_t err;           // AXC_ERR_* bits, sticky until read with clear
   uint32_t tick_base;     // batch mode: global tick of tick 0 of the batch
   int32_t dopamine;       // batch mode: dopamine of the batch
-  uint32_t eval_count;    // row engine: non-refractory neurons listed this tick
   uint32_t fix_count;     // row engine: GSOP slots deferred to the fix-up stage
   uint32_t fix_overflow;  // row engine: the fix-up list overflowed, rescan the spikers
-  uint32_t pad;
+  uint32_t eval_count[2]; // row engine: non-refractory neurons listed in tick k (slot k & 1)
   unsigned long long ctr[8];  // statistics, see axc_shard_counters
 };
 

@@ -219,7 +219,8 @@ __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ we
 
 // ---------------------------------------------------------------------------
 // per tick 1/4: axons (inject, network pushes, propagate, split masks) and
-// somas (refractory countdown, list of neurons to evaluate).
+// somas (refractory countdown, list of neurons to evaluate).  The list entry
+// positions are reserved once per block.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__ heads, uint32_t A, uint32_t v_seg,
                                                        const uint32_t* __restrict__ bitmask, uint32_t voff,
@@ -229,13 +230,13 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint8_t* __restrict__ flags, uint8_t* __restrict__ timers,
                                                        uint32_t N, uint32_t* __restrict__ eval,
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err) {
-  __shared__ uint32_t s_pmax;
+  __shared__ uint32_t s_pmax, s_base;
   __shared__ int s_inc;
+  __shared__ uint32_t s_warp[8];
   if (threadIdx.x == 0) {
     s_pmax = lut_pmax();
     s_inc = batch_counts && batch_counts[k] > 0;
     if (blockIdx.x == 0) {
-      ctl->spike_count = 0;
       ctl->ctr[0] += 1;
       if (raise_err) atomicOr(&ctl->err, raise_err);
     }
@@ -273,15 +274,17 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
       ev = true;
     }
   }
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t ballot = __ballot_sync(kFull, ev);
-  if (ballot) {
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ballot) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(&ctl->eval_count, (uint32_t)__popc(ballot));
-    base = __shfl_sync(kFull, base, leader);
-    if (ev) eval[base + __popc(ballot & ((1u << lane) - 1u))] = i;
+  if (lane == 0) s_warp[w] = __popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int q = 0; q < 8; q++) { const uint32_t c = s_warp[q]; s_warp[q] = tot; tot += c; }
+    s_base = tot ? atomicAdd(&ctl->eval_count[k & 1], tot) : 0u;
   }
+  __syncthreads();
+  if (ev) eval[s_base + s_warp[w] + __popc(ballot & ((1u << lane) - 1u))] = i;
 }
 
 // ---------------------------------------------------------------------------
@@ -300,21 +303,51 @@ __device__ __forceinline__ void set_half(uint2& v, int i, int16_t x) {
   w = (i & 1) ? ((w & 0x0000FFFFu) | ((uint32_t)(uint16_t)x << 16)) : ((w & 0xFFFF0000u) | (uint16_t)x);
 }
 
+// Rare paths of the update pass, kept out of line so that the hot loop keeps
+// its registers.
+__device__ __noinline__ bool hit_exact(const BurstHeads8* heads, uint32_t a, uint32_t s, uint32_t prop) {
+  return heads_hit(heads, a, s, prop);
+}
+
+// General GSOP of one slot: exact distances; returns false when the slot must
+// be deferred to the fix-up stage (its result depends on same-tick pushes).
+__device__ __noinline__ bool gsop_general(const BurstHeads8* heads, const uint2* mask2, uint32_t a, uint32_t s,
+                                          const VariantParameters& p, uint8_t flags, int32_t dopamine,
+                                          int16_t* w16) {
+  const uint2 m = __ldg(mask2 + a);
+  uint32_t md, md1;
+  md_pair(heads, a, s, p.signal_propagation_length, &md, &md1);
+  if ((m.y >> 31) || md != md1) return false;
+  const GsopConsts gc = gsop_consts((uint8_t)((flags & 0xF0) | 0x05), p, dopamine);
+  *w16 = gsop_weight(*w16, md, p, gc.bm, gc.raw_pot, gc.final_dep);
+  return true;
+}
+
 __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A,
                                                         const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
                                                         const uint8_t* __restrict__ cnt,
                                                         const uint2* __restrict__ mask2,
                                                         const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend,
-                                                        uint32_t* __restrict__ spikers, uint32_t* __restrict__ fix,
-                                                        ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap) {
+                                                        uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
+                                                        uint32_t k, uint32_t fix_cap) {
   __shared__ VariantParameters lut[16];
+  __shared__ int2 gtab[16][16];   // GSOP (potentiation, depression) per variant and inertia rank
   __shared__ uint32_t s_pmax;
   lut_to_smem(lut);
   if (threadIdx.x == 0) s_pmax = lut_pmax();
   __syncthreads();
   const uint32_t tick = ctl->tick_base + k;
   const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
-  const uint32_t ecount = ctl->eval_count;
+  {
+    // a spiker's flags after the update are type | 0b101, so its burst multiplier
+    // is 2 (physics.cu:255, 271-273, 290-291); physics.cu:336-349 for each rank
+    const uint32_t v = threadIdx.x >> 4, r = threadIdx.x & 15;
+    const GsopConsts g = gsop_consts((uint8_t)((v << 4) | 0x05), lut[v], dopamine);
+    const int32_t inertia = lut[v].inertia_curve[r];
+    gtab[v][r] = make_int2(wmul(wmul(g.raw_pot, inertia), g.bm) >> 7, wmul(wmul(g.final_dep, inertia), g.bm) >> 7);
+  }
+  __syncthreads();
+  const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -325,13 +358,13 @@ __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_
     const uint32_t n = valid ? eval[idx] : 0u;
     const uint8_t flags = valid ? P.soma_flags[n] : 0;
     const uint32_t c = valid ? cnt[n] : 0u;
-    const VariantParameters& p = lut[flags >> 4];
+    const uint32_t var = flags >> 4;
+    const VariantParameters& p = lut[var];
     const uint32_t prop = p.signal_propagation_length;
     const bool exact = prop == s_pmax;
     const bool gfast = exact && prop <= 16u;
     const uint32_t* trow = rt + (size_t)n * kRowStride + 4u * g8;
-    const int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
-    // all four chunks of the row in flight at once
+    int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
     uint4 T[4];
     uint2 W[4];
 #pragma unroll
@@ -350,41 +383,37 @@ __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_
     for (int j = 0; j < 4; j++) {
       const uint32_t q0 = 32u * j + 4u * g8;
       uint2 m[4];
-      uint32_t ax[4];
       bool ok[4];
 #pragma unroll
       for (int i = 0; i < 4; i++) {
-        ax[i] = (word_of(T[j], i) & AXC_TARGET_AXON_MASK) - 1u;
+        const uint32_t ax = (word_of(T[j], i) & AXC_TARGET_AXON_MASK) - 1u;
         const bool live = q0 + i < c;
-        ok[i] = live && ax[i] < A;
-        if (live && !ok[i]) badb |= 1u << (4 * j + i);
-        m[i] = ok[i] ? __ldg(mask2 + ax[i]) : make_uint2(0, 0);
+        ok[i] = live && ax < A;
+        badb |= (live && !ok[i]) ? (1u << (4 * j + i)) : 0u;
+        m[i] = ok[i] ? __ldg(mask2 + ax) : make_uint2(0, 0);
       }
 #pragma unroll
       for (int i = 0; i < 4; i++) {
-        if (!ok[i]) continue;
-        const uint32_t s = word_of(T[j], i) >> AXC_TARGET_SEG_SHIFT;
-        bool hit;
-        if (s < 31u) {
-          hit = ((m[i].x | m[i].y) >> s) & 1u;
-          if (hit && !exact) hit = heads_hit(P.axon_heads, ax[i], s, prop);
-        } else {
-          hit = (m[i].x >> 31) && heads_hit(P.axon_heads, ax[i], s, prop);
-        }
+        const uint32_t t = word_of(T[j], i);
+        const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+        const uint32_t sh = min(s, 31u);
+        const uint32_t bx = (m[i].x >> sh) & 1u, by = (m[i].y >> sh) & 1u;
+        bool hit = (bx | by) != 0u;                 // bit 31 (s >= 31): "may hit", tested below
+        if (hit && (s >= 31u || !exact)) hit = hit_exact(P.axon_heads, (t & AXC_TARGET_AXON_MASK) - 1u, s, prop);
         if (hit) {
           i_in = wadd(i_in, (int32_t)half_of(W[j], i));
           hitb |= 1u << (4 * j + i);
         }
-        if (!fast_class(s, m[i], gfast) || fast_sensitive(s, m[i])) slowb |= 1u << (4 * j + i);
+        // fast GSOP: hit decides, and one same-tick push could not change it
+        const bool fast = gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u));
+        slowb |= (ok[i] && !fast) ? (1u << (4 * j + i)) : 0u;
       }
     }
     if (badb) err |= AXC_ERR_TARGET_RANGE;
-    // sum over the 8 lanes of the neuron
     i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
     i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
     i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
-    ev_slots += (g8 == 0) ? c : 0u;
-    nev += (valid && g8 == 0) ? 1u : 0u;
+    if (g8 == 0) { ev_slots += c; nev += valid ? 1u : 0u; }
     hits += __popc(hitb);
     // GLIF (physics.cu:209-275); the neuron is not refractory
     int spike = 0;
@@ -418,6 +447,7 @@ __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_
         P.threshold_offset[n] = thr;
         P.timers[n] = glif ? p.refractory_period : 0;
         if (spike) {
+          nspk++;
           const uint32_t my_axon = P.soma_to_axon[n];
           if (my_axon != AXC_NO_AXON) {
             if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
@@ -426,52 +456,40 @@ __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_
         }
       }
     }
-    // spiker list (one entry per neuron, from its lane 0)
-    const uint32_t lead = __ballot_sync(kFull, spike && g8 == 0);
-    if (lead) {
-      const int leader = __ffs(lead) - 1;
-      uint32_t b0 = 0;
-      if ((int)lane == leader) b0 = atomicAdd(&ctl->spike_count, (uint32_t)__popc(lead));
-      b0 = __shfl_sync(kFull, b0, leader);
-      if (spike && g8 == 0) spikers[b0 + __popc(lead & ((1u << lane) - 1u))] = n;
-      nspk += (spike && g8 == 0) ? 1u : 0u;
-    }
-    // GSOP on the same rows (physics.cu:281-373); the chunks are reloaded from L1
+    // GSOP on the row in registers (physics.cu:281-373)
     if (spike) {
-      const GsopConsts gc = gsop_consts((uint8_t)((flags & 0xF0) | 0x05), p, dopamine);
-#pragma unroll 1
+#pragma unroll
       for (int j = 0; j < 4; j++) {
         const uint32_t q0 = 32u * j + 4u * g8;
-        if (q0 >= c) break;
-        const uint4 tj = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
-        uint2 wj = *reinterpret_cast<const uint2*>(wrow + 32 * j);
-        bool dirty = false;
+        if (q0 >= c) continue;
+        uint2 wj = W[j];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           const uint32_t b = 1u << (4 * j + i);
           if (q0 + i >= c || (badb & b)) continue;
           gdone++;
-          uint32_t md;
+          const int16_t w16 = half_of(wj, i);
           if (!(slowb & b)) {
-            md = (hitb & b) ? 0u : kInf;
-          } else {
-            const uint32_t t = word_of(tj, i);
-            const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
-            const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
-            const uint2 m = __ldg(mask2 + a);
-            uint32_t md1;
-            md_pair(P.axon_heads, a, s, prop, &md, &md1);
-            if ((m.y >> 31) || md != md1) {
-              const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
-              if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
-              else ctl->fix_overflow = 1u;
-              continue;
-            }
+            // cooling shift 0: delta = +potentiation or -depression of the weight's rank
+            const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+            const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
+            int32_t na = aw + ((hitb & b) ? e.x : -e.y);
+            na = min(max(na, 0), 32767);
+            set_half(wj, i, (int16_t)(w16 < 0 ? -na : na));
+            continue;
           }
-          set_half(wj, i, gsop_weight(half_of(wj, i), md, p, gc.bm, gc.raw_pot, gc.final_dep));
-          dirty = true;
+          const uint32_t t = __ldg(trow + 32 * j + i);   // T[] is dead after the gather: reload (L1)
+          int16_t nw = w16;
+          if (!gsop_general(P.axon_heads, mask2, (t & AXC_TARGET_AXON_MASK) - 1u, t >> AXC_TARGET_SEG_SHIFT, p,
+                            flags, dopamine, &nw)) {
+            const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+            if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
+            else ctl->fix_overflow = 1u;
+            continue;
+          }
+          set_half(wj, i, nw);
         }
-        if (dirty) *reinterpret_cast<uint2*>(rw + (size_t)n * kRowStride + q0) = wj;
+        if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
       }
     }
   }
@@ -483,7 +501,7 @@ __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_
 
 // ---------------------------------------------------------------------------
 // per tick 3/4: deferred GSOP slots, with the actual push count of the axon
-// (pend, before k_push consumes it) and the original weight.
+// (pend, before the push stage consumes it) and the original weight.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void fixup_slot(const ShardVramPtrs& P, const VariantParameters* lut, uint32_t A,
                                            const uint32_t* rt, int16_t* rw, const uint32_t* pend,
@@ -506,8 +524,9 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
                                                     const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
                                                     const uint8_t* __restrict__ cnt,
                                                     const uint2* __restrict__ mask2, const uint32_t* __restrict__ pend,
-                                                    const uint32_t* __restrict__ spikers,
-                                                    const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl) {
+                                                    const uint32_t* __restrict__ eval,
+                                                    const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
+                                                    uint32_t k) {
   const uint32_t nfix = ctl->fix_count;
   const uint32_t overflow = ctl->fix_overflow;
   if (nfix == 0 && !overflow) return;
@@ -524,10 +543,10 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
     return;
   }
   // the list overflowed: rescan every spiker's slots with the update pass's rule
-  const uint32_t nsp = ctl->spike_count;
-  for (uint32_t w = tid; w < nsp * kRowStride; w += stride) {
-    const uint32_t n = spikers[w / kRowStride], q = w % kRowStride;
-    if (q >= cnt[n]) continue;
+  const uint32_t ecount = ctl->eval_count[k & 1];
+  for (uint32_t w = tid; w < ecount * kRowStride; w += stride) {
+    const uint32_t n = eval[w / kRowStride], q = w % kRowStride;
+    if (!(P.soma_flags[n] & 1) || q >= cnt[n]) continue;
     const uint32_t r = n * kRowStride + q;
     const uint32_t t = rt[r];
     const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
@@ -537,20 +556,62 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
     const uint32_t prop = p.signal_propagation_length;
     const bool gfast = prop == s_pmax && prop <= 16u;
     const uint2 m = mask2[a];
-    bool defer;
-    if (fast_class(s, m, gfast) && !fast_sensitive(s, m)) {
-      defer = false;
-    } else {
-      uint32_t md0, md1;
-      md_pair(P.axon_heads, a, s, prop, &md0, &md1);
-      defer = (m.y >> 31) || md0 != md1;
-    }
-    if (defer) fixup_slot(P, lut, A, rt, rw, pend, r, dopamine);
+    const uint32_t sh = min(s, 31u);
+    const uint32_t bx = (m.x >> sh) & 1u, by = (m.y >> sh) & 1u;
+    const bool fast = gfast && s < 31u && !(m.y >> 31) && (bx || by == (s == 0u));
+    if (fast) continue;
+    uint32_t md0, md1;
+    md_pair(P.axon_heads, a, s, prop, &md0, &md1);
+    if ((m.y >> 31) || md0 != md1) fixup_slot(P, lut, A, rt, rw, pend, r, dopamine);
   }
 }
 
+// per tick 4/4: the spikers' own-axon pushes (physics.cu:257-261), found in
+// the evaluated list; readout (physics.cu:378-395); the next tick's lists.
+__global__ void __launch_bounds__(256) k_rows_push(BurstHeads8* __restrict__ heads, const uint32_t* __restrict__ s2a,
+                                                   uint32_t A, uint32_t* __restrict__ pend,
+                                                   const uint32_t* __restrict__ eval, const uint8_t* __restrict__ flags,
+                                                   uint32_t N, const uint32_t* __restrict__ ids,
+                                                   uint8_t* __restrict__ out, uint32_t num_outputs,
+                                                   ShardCtl* __restrict__ ctl, uint32_t k) {
+  const uint32_t ecount = ctl->eval_count[k & 1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid == 0) {
+    ctl->eval_count[(k + 1) & 1] = 0;
+    ctl->fix_count = 0;
+    ctl->fix_overflow = 0;
+  }
+  for (uint32_t i = tid; i < ecount; i += stride) {
+    const uint32_t n = eval[i];
+    if (!(flags[n] & 1)) continue;
+    const uint32_t ax = s2a[n];
+    if (ax >= A) continue;
+    const uint32_t c = atomicExch(&pend[ax], 0u);
+    if (!c) continue;
+    uint4* p = reinterpret_cast<uint4*>(heads + ax);
+    uint4 x = p[0], y = p[1];
+    uint32_t h[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+    push_n(h, c);
+    p[0] = make_uint4(h[0], h[1], h[2], h[3]);
+    p[1] = make_uint4(h[4], h[5], h[6], h[7]);
+  }
+  uint32_t err = 0;
+  for (uint32_t j = tid; j < num_outputs; j += stride) {
+    const uint32_t id = ids[j];
+    uint8_t v = 0;
+    if (id != AXC_NO_AXON) {
+      if (id < N) v = flags[id] & 0x01;
+      else err = AXC_ERR_READOUT_RANGE;
+    }
+    out[j] = v;
+  }
+  if (err) atomicOr(&ctl->err, err);
+}
+
 __global__ void k_rows_reset_lists(ShardCtl* ctl) {
-  ctl->eval_count = 0;
+  ctl->eval_count[0] = 0;
+  ctl->eval_count[1] = 0;
   ctl->fix_count = 0;
   ctl->fix_overflow = 0;
 }
@@ -626,13 +687,14 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
         raise);
   if (ev) cudaEventRecord(ev[2], stream);
-  k_rows_update<<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, s.spikers, r.fix,
-                                             s.ctl, a.k, min(a.fix_cap, kFixCap));
+  k_rows_update<<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, a.k,
+                                             min(a.fix_cap, kFixCap));
   if (ev) cudaEventRecord(ev[3], stream);
-  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, s.spikers, r.fix, s.ctl);
+  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
-  k_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, s.spikers, s.ctl, v.soma_flags, N,
-                                      a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0);
+  k_rows_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, r.eval, v.soma_flags, N,
+                                           a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0, s.ctl,
+                                           a.k);
   if (ev) {
     cudaEventRecord(ev[4], stream);
     cudaEventRecord(ev[5], stream);
