@@ -17,6 +17,8 @@ struct ShardCtl {
   uint32_t fix_count;     // row engine: GSOP slots deferred to the fix-up stage
   uint32_t fix_overflow;  // row engine: the fix-up list overflowed, rescan the spikers
   uint32_t eval_count[2]; // row engine: non-refractory neurons listed in tick k (slot k & 1)
+  uint32_t row_smax;      // row engine: longest row (slots before the first empty) of the batch
+  uint32_t pad[3];
   unsigned long long ctr[8];  // statistics, see axc_shard_counters
 };
 
@@ -27,8 +29,8 @@ struct RowCache {
   void* base = nullptr;
   uint32_t* rt = nullptr;   // [N][128] targets, neuron-major
   int16_t* rw = nullptr;    // [N][128] weights, neuron-major
-  uint8_t* cnt = nullptr;   // [N] slots before the first empty target
-  uint2* mask2 = nullptr;   // [A] split segment-hit masks (heads 0..6 | head 7)
+  uint16_t* cnt = nullptr;  // [N] slots before the first empty target; bit 15: an invalid target
+  uint2* mask2 = nullptr;   // [A+1] split segment-hit masks (heads 0..6 | head 7); [A] dummy
   uint32_t* mult = nullptr; // [A] number of somas that own the axon
   uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)

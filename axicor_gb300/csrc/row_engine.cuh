@@ -36,6 +36,7 @@ namespace {
 
 constexpr uint32_t kRowStride = AXC_MAX_DENDRITES;   // slots per neuron row
 constexpr uint32_t kInf = 0xFFFFFFFFu;
+constexpr uint32_t kRowBad = 0x8000u;    // cnt flag: the row holds an invalid target
 
 // physics.cu:322-371 for one slot given the minimum in-tail distance md.
 __device__ __forceinline__ int16_t gsop_weight(int16_t w16, uint32_t md, const VariantParameters& p, int32_t bm,
@@ -151,7 +152,7 @@ __device__ __forceinline__ bool fast_sensitive(uint32_t s, uint2 m) {
 __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__ targets,
                                                     const int16_t* __restrict__ weights, uint32_t N,
                                                     uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
-                                                    uint8_t* __restrict__ cnt) {
+                                                    uint16_t* __restrict__ cnt, ShardCtl* __restrict__ ctl, uint32_t A) {
   __shared__ uint32_t s_t[AXC_MAX_DENDRITES][33];
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_cnt[32];
@@ -179,17 +180,34 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     const uint32_t n = n0 + j;
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
+    bool bad = false;
     for (uint32_t q = lane; q < c; q += 32) {
-      rt[(size_t)n * kRowStride + q] = s_t[q][j];
+      uint32_t t = s_t[q][j];
+      // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
+      // which sends the slot down the exact path (hit_exact / gsop_general skip it)
+      if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
+        t = (t & ~AXC_TARGET_AXON_MASK) | (A + 1u);
+        bad = true;
+      }
+      rt[(size_t)n * kRowStride + q] = t;
       rw[(size_t)n * kRowStride + q] = s_w[q][j];
     }
-    if (lane == 0) cnt[n] = (uint8_t)min(c, 255u);
+    bad = __any_sync(kFull, bad);
+    if (lane == 0) {
+      cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
+      if (c) atomicMax(&ctl->row_smax, c);
+    }
   }
 }
 
 __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ s2a, uint32_t N, uint32_t A,
-                                                   uint32_t* __restrict__ mult) {
+                                                   uint32_t* __restrict__ mult, uint2* __restrict__ mask2,
+                                                   ShardCtl* __restrict__ ctl) {
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n == 0) {
+    mask2[A] = make_uint2(0u, 0x80000000u);   // dummy entry of invalid targets: no hit, exact path
+    ctl->row_smax = 0;
+  }
   if (n >= N) return;
   const uint32_t a = s2a[n];
   if (a < A) atomicAdd(&mult[a], 1u);
@@ -198,14 +216,14 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
 // batch end: weights rows -> columnar for slots before the first empty target.
 __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ weights, uint32_t N,
                                                         const int16_t* __restrict__ rw,
-                                                        const uint8_t* __restrict__ cnt) {
+                                                        const uint16_t* __restrict__ cnt) {
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_c[32];
   const uint32_t n0 = blockIdx.x * 32;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint32_t j = warp; j < 32; j += 8) {
     const uint32_t n = n0 + j;
-    const uint32_t c = n < N ? cnt[n] : 0u;
+    const uint32_t c = n < N ? (cnt[n] & 0xFFu) : 0u;
     if (lane == 0) s_c[j] = c;
     for (uint32_t q = lane; q < c; q += 32) s_w[q][j] = rw[(size_t)n * kRowStride + q];
   }
@@ -305,27 +323,31 @@ __device__ __forceinline__ void set_half(uint2& v, int i, int16_t x) {
 
 // Rare paths of the update pass, kept out of line so that the hot loop keeps
 // its registers.
-__device__ __noinline__ bool hit_exact(const BurstHeads8* heads, uint32_t a, uint32_t s, uint32_t prop) {
-  return heads_hit(heads, a, s, prop);
+__device__ __noinline__ bool hit_exact(const BurstHeads8* heads, uint32_t A, uint32_t a, uint32_t s,
+                                       uint32_t prop) {
+  return a < A && heads_hit(heads, a, s, prop);
 }
 
-// General GSOP of one slot: exact distances; returns false when the slot must
-// be deferred to the fix-up stage (its result depends on same-tick pushes).
-__device__ __noinline__ bool gsop_general(const BurstHeads8* heads, const uint2* mask2, uint32_t a, uint32_t s,
-                                          const VariantParameters& p, uint8_t flags, int32_t dopamine,
-                                          int16_t* w16) {
+// General GSOP of one slot with exact distances.  Returns 0 when applied, 1
+// when the slot must be deferred to the fix-up stage (its result depends on
+// same-tick pushes), 2 when the target is invalid (skipped, physics.cu would
+// read out of bounds).
+__device__ __noinline__ int gsop_general(const BurstHeads8* heads, const uint2* mask2, uint32_t A, uint32_t a,
+                                         uint32_t s, const VariantParameters& p, uint8_t flags, int32_t dopamine,
+                                         int16_t* w16) {
+  if (a >= A) return 2;
   const uint2 m = __ldg(mask2 + a);
   uint32_t md, md1;
   md_pair(heads, a, s, p.signal_propagation_length, &md, &md1);
-  if ((m.y >> 31) || md != md1) return false;
+  if ((m.y >> 31) || md != md1) return 1;
   const GsopConsts gc = gsop_consts((uint8_t)((flags & 0xF0) | 0x05), p, dopamine);
   *w16 = gsop_weight(*w16, md, p, gc.bm, gc.raw_pot, gc.final_dep);
-  return true;
+  return 0;
 }
 
 __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A,
                                                         const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
-                                                        const uint8_t* __restrict__ cnt,
+                                                        const uint16_t* __restrict__ cnt,
                                                         const uint2* __restrict__ mask2,
                                                         const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend,
                                                         uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
@@ -348,148 +370,158 @@ __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_
   }
   __syncthreads();
   const uint32_t ecount = ctl->eval_count[k & 1];
+  const uint32_t smax = ctl->row_smax;   // longest row of the shard: rows are loaded up to here
   const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // each warp owns a contiguous slice of the list, 4 neurons per step
+  const uint32_t per_warp = (((ecount + nwarps - 1) / nwarps) + 3) & ~3u;
+  const uint32_t beg = min(wid * per_warp, ecount), end = min(beg + per_warp, ecount);
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
-  for (uint32_t base = wid * 4; base < ecount; base += nwarps * 4) {
-    const uint32_t idx = base + grp;
-    const bool valid = idx < ecount;
-    const uint32_t n = valid ? eval[idx] : 0u;
-    const uint8_t flags = valid ? P.soma_flags[n] : 0;
-    const uint32_t c = valid ? cnt[n] : 0u;
-    const uint32_t var = flags >> 4;
-    const VariantParameters& p = lut[var];
-    const uint32_t prop = p.signal_propagation_length;
-    const bool exact = prop == s_pmax;
-    const bool gfast = exact && prop <= 16u;
-    const uint32_t* trow = rt + (size_t)n * kRowStride + 4u * g8;
-    int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
-    uint4 T[4];
-    uint2 W[4];
+  for (uint32_t base = beg; base < end; base += 32) {
+    const uint32_t mine = (base + lane < end) ? __ldg(eval + base + lane) : 0u;
+    for (uint32_t sub = 0; sub < 32 && base + sub < end; sub += 4) {
+      const bool valid = base + sub + grp < end;
+      const uint32_t n = __shfl_sync(kFull, mine, sub + grp);
+      // every load of the neuron at once: state, count, and its row up to smax
+      const uint8_t flags = P.soma_flags[n];
+      const uint32_t cw = valid ? cnt[n] : 0u;
+      const int32_t thr0 = P.threshold_offset[n];
+      const int32_t v0 = P.soma_voltage[n];
+      const uint32_t* trow = rt + (size_t)n * kRowStride + 4u * g8;
+      int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
+      uint4 T[4];
+      uint2 W[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      if (32u * j + 4u * g8 < c) {
-        T[j] = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
-        W[j] = *reinterpret_cast<const uint2*>(wrow + 32 * j);
-      } else {
-        T[j] = make_uint4(0, 0, 0, 0);
-        W[j] = make_uint2(0, 0);
-      }
-    }
-    int32_t i_in = 0;
-    uint32_t hitb = 0, slowb = 0, badb = 0;   // bit 4j+i
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const uint32_t q0 = 32u * j + 4u * g8;
-      uint2 m[4];
-      bool ok[4];
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const uint32_t ax = (word_of(T[j], i) & AXC_TARGET_AXON_MASK) - 1u;
-        const bool live = q0 + i < c;
-        ok[i] = live && ax < A;
-        badb |= (live && !ok[i]) ? (1u << (4 * j + i)) : 0u;
-        m[i] = ok[i] ? __ldg(mask2 + ax) : make_uint2(0, 0);
-      }
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const uint32_t t = word_of(T[j], i);
-        const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
-        const uint32_t sh = min(s, 31u);
-        const uint32_t bx = (m[i].x >> sh) & 1u, by = (m[i].y >> sh) & 1u;
-        bool hit = (bx | by) != 0u;                 // bit 31 (s >= 31): "may hit", tested below
-        if (hit && (s >= 31u || !exact)) hit = hit_exact(P.axon_heads, (t & AXC_TARGET_AXON_MASK) - 1u, s, prop);
-        if (hit) {
-          i_in = wadd(i_in, (int32_t)half_of(W[j], i));
-          hitb |= 1u << (4 * j + i);
-        }
-        // fast GSOP: hit decides, and one same-tick push could not change it
-        const bool fast = gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u));
-        slowb |= (ok[i] && !fast) ? (1u << (4 * j + i)) : 0u;
-      }
-    }
-    if (badb) err |= AXC_ERR_TARGET_RANGE;
-    i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
-    i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
-    i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
-    if (g8 == 0) { ev_slots += c; nev += valid ? 1u : 0u; }
-    hits += __popc(hitb);
-    // GLIF (physics.cu:209-275); the neuron is not refractory
-    int spike = 0;
-    if (valid) {
-      int32_t thr = P.threshold_offset[n];
-      const int32_t decayed = wsub(thr, (int32_t)p.homeostasis_decay);
-      thr = decayed & ~(decayed >> 31);
-      int32_t leak = p.leak_rate;
-      if (p.adaptive_mode == 1) {
-        leak = wadd(leak, wmul(thr, (int32_t)p.adaptive_leak_gain) >> 8);
-        const int32_t over = wsub(leak, p.adaptive_leak_max);
-        leak = wsub(leak, over & ~(over >> 31));
-      }
-      int32_t v = wadd(P.soma_voltage[n], i_in);
-      const int32_t diff = wsub(v, p.rest_potential);
-      const int32_t sign = (diff > 0) - (diff < 0);
-      int32_t leaked = wsub(wmul(diff, sign), leak);
-      leaked = leaked & ~(leaked >> 31);
-      v = wadd(p.rest_potential, wmul(sign, leaked));
-      const int glif = v >= wadd(p.threshold, thr) ? 1 : 0;
-      const uint32_t period = p.spontaneous_firing_period_ticks;
-      const int hb = (period > 0 && ((tick + n * 104729u) % period) == 0) ? 1 : 0;
-      spike = glif | hb;
-      if (glif) {
-        v = p.rest_potential;
-        thr = wadd(thr, p.homeostasis_penalty);
-      }
-      if (g8 == 0) {
-        P.soma_voltage[n] = v;
-        P.soma_flags[n] = (uint8_t)((flags & 0xF0) | (spike ? 0x05 : 0x00));
-        P.threshold_offset[n] = thr;
-        P.timers[n] = glif ? p.refractory_period : 0;
-        if (spike) {
-          nspk++;
-          const uint32_t my_axon = P.soma_to_axon[n];
-          if (my_axon != AXC_NO_AXON) {
-            if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
-            else err |= AXC_ERR_SOMA_AXON;
-          }
+      for (int j = 0; j < 4; j++) {
+        if (valid && 32u * j + 4u * g8 < smax) {
+          T[j] = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
+          W[j] = *reinterpret_cast<const uint2*>(wrow + 32 * j);
+        } else {
+          T[j] = make_uint4(0, 0, 0, 0);
+          W[j] = make_uint2(0, 0);
         }
       }
-    }
-    // GSOP on the row in registers (physics.cu:281-373)
-    if (spike) {
+      const uint32_t c = cw & 0xFFu;
+      const uint32_t var = flags >> 4;
+      const VariantParameters& p = lut[var];
+      const uint32_t prop = p.signal_propagation_length;
+      const bool exact = prop == s_pmax;
+      const bool gfast = exact && prop <= 16u;
+      if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
+      int32_t i_in = 0;
+      uint32_t hitb = 0, slowb = 0;   // bit 4j+i
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const uint32_t q0 = 32u * j + 4u * g8;
-        if (q0 >= c) continue;
-        uint2 wj = W[j];
+        uint2 m[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          const uint32_t b = 1u << (4 * j + i);
-          if (q0 + i >= c || (badb & b)) continue;
-          gdone++;
-          const int16_t w16 = half_of(wj, i);
-          if (!(slowb & b)) {
-            // cooling shift 0: delta = +potentiation or -depression of the weight's rank
-            const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
-            const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
-            int32_t na = aw + ((hitb & b) ? e.x : -e.y);
-            na = min(max(na, 0), 32767);
-            set_half(wj, i, (int16_t)(w16 < 0 ? -na : na));
-            continue;
-          }
-          const uint32_t t = __ldg(trow + 32 * j + i);   // T[] is dead after the gather: reload (L1)
-          int16_t nw = w16;
-          if (!gsop_general(P.axon_heads, mask2, (t & AXC_TARGET_AXON_MASK) - 1u, t >> AXC_TARGET_SEG_SHIFT, p,
-                            flags, dopamine, &nw)) {
-            const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
-            if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
-            else ctl->fix_overflow = 1u;
-            continue;
-          }
-          set_half(wj, i, nw);
+          const uint32_t ax = (word_of(T[j], i) & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
+          m[i] = (q0 + i < c) ? __ldg(mask2 + ax) : make_uint2(0, 0);
         }
-        if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          if (q0 + i >= c) continue;
+          const uint32_t t = word_of(T[j], i);
+          const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+          const uint32_t sh = min(s, 31u);
+          const uint32_t bx = (m[i].x >> sh) & 1u, by = (m[i].y >> sh) & 1u;
+          bool hit = (bx | by) != 0u;              // bit 31 (s >= 31): "may hit", tested below
+          if (hit && (s >= 31u || !exact))
+            hit = hit_exact(P.axon_heads, A, (t & AXC_TARGET_AXON_MASK) - 1u, s, prop);
+          if (hit) {
+            i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+            hitb |= 1u << (4 * j + i);
+          }
+          // fast GSOP: hit decides, and one same-tick push could not change it
+          const bool fast = gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u));
+          slowb |= fast ? 0u : (1u << (4 * j + i));
+        }
+      }
+      i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
+      i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
+      i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
+      if (g8 == 0 && valid) { ev_slots += c; nev++; }
+      hits += __popc(hitb);
+      // GLIF (physics.cu:209-275); the neuron is not refractory
+      int spike = 0;
+      if (valid) {
+        const int32_t decayed = wsub(thr0, (int32_t)p.homeostasis_decay);
+        int32_t thr = decayed & ~(decayed >> 31);
+        int32_t leak = p.leak_rate;
+        if (p.adaptive_mode == 1) {
+          leak = wadd(leak, wmul(thr, (int32_t)p.adaptive_leak_gain) >> 8);
+          const int32_t over = wsub(leak, p.adaptive_leak_max);
+          leak = wsub(leak, over & ~(over >> 31));
+        }
+        int32_t v = wadd(v0, i_in);
+        const int32_t diff = wsub(v, p.rest_potential);
+        const int32_t sign = (diff > 0) - (diff < 0);
+        int32_t leaked = wsub(wmul(diff, sign), leak);
+        leaked = leaked & ~(leaked >> 31);
+        v = wadd(p.rest_potential, wmul(sign, leaked));
+        const int glif = v >= wadd(p.threshold, thr) ? 1 : 0;
+        const uint32_t period = p.spontaneous_firing_period_ticks;
+        const int hb = (period > 0 && ((tick + n * 104729u) % period) == 0) ? 1 : 0;
+        spike = glif | hb;
+        if (glif) {
+          v = p.rest_potential;
+          thr = wadd(thr, p.homeostasis_penalty);
+        }
+        if (g8 == 0) {
+          P.soma_voltage[n] = v;
+          P.soma_flags[n] = (uint8_t)((flags & 0xF0) | (spike ? 0x05 : 0x00));
+          P.threshold_offset[n] = thr;
+          P.timers[n] = glif ? p.refractory_period : 0;
+          if (spike) {
+            nspk++;
+            const uint32_t my_axon = P.soma_to_axon[n];
+            if (my_axon != AXC_NO_AXON) {
+              if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
+              else err |= AXC_ERR_SOMA_AXON;
+            }
+          }
+        }
+      }
+      // GSOP on the row in registers (physics.cu:281-373)
+      if (spike) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const uint32_t q0 = 32u * j + 4u * g8;
+          if (q0 >= c) continue;
+          uint2 wj = W[j];
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            const uint32_t b = 1u << (4 * j + i);
+            if (q0 + i >= c) continue;
+            const int16_t w16 = half_of(wj, i);
+            if (!(slowb & b)) {
+              // cooling shift 0: delta = +potentiation or -depression of the weight's rank
+              const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+              const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
+              int32_t na = aw + ((hitb & b) ? e.x : -e.y);
+              na = min(max(na, 0), 32767);
+              set_half(wj, i, (int16_t)(w16 < 0 ? -na : na));
+              gdone++;
+              continue;
+            }
+            const uint32_t t = __ldg(trow + 32 * j + i);
+            int16_t nw = w16;
+            const int r = gsop_general(P.axon_heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u,
+                                       t >> AXC_TARGET_SEG_SHIFT, p, flags, dopamine, &nw);
+            if (r == 2) continue;
+            gdone++;
+            if (r == 1) {
+              const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+              if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
+              else ctl->fix_overflow = 1u;
+              continue;
+            }
+            set_half(wj, i, nw);
+          }
+          if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
+        }
       }
     }
   }
@@ -522,7 +554,7 @@ __device__ __forceinline__ void fixup_slot(const ShardVramPtrs& P, const Variant
 
 __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N, uint32_t A,
                                                     const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
-                                                    const uint8_t* __restrict__ cnt,
+                                                    const uint16_t* __restrict__ cnt,
                                                     const uint2* __restrict__ mask2, const uint32_t* __restrict__ pend,
                                                     const uint32_t* __restrict__ eval,
                                                     const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
@@ -546,7 +578,7 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
   const uint32_t ecount = ctl->eval_count[k & 1];
   for (uint32_t w = tid; w < ecount * kRowStride; w += stride) {
     const uint32_t n = eval[w / kRowStride], q = w % kRowStride;
-    if (!(P.soma_flags[n] & 1) || q >= cnt[n]) continue;
+    if (!(P.soma_flags[n] & 1) || q >= (cnt[n] & 0xFFu)) continue;
     const uint32_t r = n * kRowStride + q;
     const uint32_t t = rt[r];
     const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
@@ -625,8 +657,8 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A) {
   size_t off = 0;
   const size_t o_rt = off; off = al(off + (size_t)N * kRowStride * 4);
   const size_t o_rw = off; off = al(off + (size_t)N * kRowStride * 2);
-  const size_t o_cnt = off; off = al(off + (size_t)N);
-  const size_t o_m2 = off; off = al(off + (size_t)A * 8);
+  const size_t o_cnt = off; off = al(off + (size_t)N * 2);
+  const size_t o_m2 = off; off = al(off + ((size_t)A + 1) * 8);
   const size_t o_mult = off; off = al(off + (size_t)A * 4);
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_fix = off; off = al(off + (size_t)kFixCap * 4);
@@ -642,7 +674,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A) {
   r->base = base;
   r->rt = reinterpret_cast<uint32_t*>(b + o_rt);
   r->rw = reinterpret_cast<int16_t*>(b + o_rw);
-  r->cnt = reinterpret_cast<uint8_t*>(b + o_cnt);
+  r->cnt = reinterpret_cast<uint16_t*>(b + o_cnt);
   r->mask2 = reinterpret_cast<uint2*>(b + o_m2);
   r->mult = reinterpret_cast<uint32_t*>(b + o_mult);
   r->eval = reinterpret_cast<uint32_t*>(b + o_eval);
@@ -664,8 +696,9 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
   cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
   if (e != cudaSuccess) return e;
   if (N) {
-    k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult);
-    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt);
+    k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
+    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt,
+                                                    s.ctl, A);
   }
   return cudaGetLastError();
 }

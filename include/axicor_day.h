@@ -319,6 +319,51 @@ int32_t axc_extract_outgoing_spikes_noalloc(const BurstHeads8* axon_heads,
                                             uint32_t sync_batch_ticks, uint32_t v_seg,
                                             void* out_events, uint32_t* out_count, void* stream);
 
+/* ---- Batched population ------------------------------------------------ */
+/* Many independent brains stepped together: every tick runs one launch per
+ * stage for the whole population (axons + somas, update + GSOP, GSOP fix-up,
+ * pushes), captured once into a CUDA graph of `ticks_per_graph` ticks.  Each
+ * brain keeps its own state, heads, LUT, input bitmask and tick numbering, and
+ * evolves exactly as if it ran alone through axc_step_day_phase_batch.  No
+ * counterpart in the reference (which runs one brain per shard thread). */
+typedef struct AxcPopBrainDesc {
+  ShardVramPtrs vram;                 /* from cu_allocate_shard, state uploaded */
+  uint32_t padded_n, total_axons;
+  uint32_t virtual_offset, num_virtual;
+  const uint32_t* d_input_bitmask;    /* device [ticks][words_per_tick], or NULL */
+  uint32_t words_per_tick;
+  uint32_t v_seg;
+  const VariantParameters* d_lut;     /* device, 16 entries, this brain's LUT */
+  int32_t dopamine;
+  uint32_t tick_base;                 /* global tick of bitmask row 0 */
+} AxcPopBrainDesc;
+
+/* Kernel schedule of the population stages (chosen by axc_population_tune). */
+typedef struct AxcPopSchedule {
+  uint32_t lanes_per_neuron;   /* 8 or 16 */
+  uint32_t update_blocks_per_sm;
+  uint32_t aux_blocks_per_sm;  /* fix-up and push stages */
+} AxcPopSchedule;
+
+int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, void** out_handle);
+/* Runs ticks [tick0, tick0 + ticks) of every brain (bitmask row tick0 + t),
+ * in graphs of ticks_per_graph ticks (ticks must be a multiple), with the
+ * batch prologue/epilogue (row copy, weight write-back) once per call.
+ * Asynchronous on `stream`. */
+int32_t axc_population_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t ticks_per_graph,
+                           void* stream);
+/* Times every candidate schedule on `trial_ticks` ticks from the current
+ * state and keeps the fastest (the trial ticks advance the brains like a run
+ * would; states stay exact).  Writes the chosen schedule and, optionally, the
+ * per-candidate milliseconds (out_ms[i] for candidate i, up to max_out). */
+int32_t axc_population_tune(void* handle, uint32_t tick0, uint32_t trial_ticks, void* stream,
+                            AxcPopSchedule* chosen, float* out_ms, uint32_t max_out);
+int32_t axc_population_set_schedule(void* handle, const AxcPopSchedule* schedule);
+/* Totals since creation: [0] ticks, [1] evaluated slots, [2] hits, [3] spikes,
+ * [4] GSOP slots, [5] evaluated neurons; plus [6] the error bits of all brains. */
+int32_t axc_population_counters(void* handle, uint64_t out[8]);
+void axc_population_destroy(void* handle);
+
 /* ---- Synthetic brain generator (host) ---------------------------------- */
 /* Neurons fill a dim_x*dim_y*dim_z voxel grid (x fastest, one per voxel);
  * neuron n owns axon n; input v owns virtual axon padded_n + v and sits on a
