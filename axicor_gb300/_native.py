@@ -82,6 +82,21 @@ class AxcIoBuffers(C.Structure):
     ]
 
 
+class AxcPopBrainDesc(C.Structure):
+    _fields_ = [
+        ("vram", ShardVramPtrs),
+        ("padded_n", C.c_uint32), ("total_axons", C.c_uint32),
+        ("virtual_offset", C.c_uint32), ("num_virtual", C.c_uint32),
+        ("d_input_bitmask", C.c_void_p), ("words_per_tick", C.c_uint32), ("v_seg", C.c_uint32),
+        ("d_lut", C.c_void_p), ("dopamine", C.c_int32), ("tick_base", C.c_uint32),
+    ]
+
+
+class AxcPopSchedule(C.Structure):
+    _fields_ = [("lanes_per_neuron", C.c_uint32), ("update_blocks_per_sm", C.c_uint32),
+                ("aux_blocks_per_sm", C.c_uint32)]
+
+
 class AxcBrainSpec(C.Structure):
     _fields_ = [
         ("dim_x", C.c_uint32), ("dim_y", C.c_uint32), ("dim_z", C.c_uint32),
@@ -152,6 +167,13 @@ SIGNATURES: dict[str, tuple] = {
     "axc_batch_engine_mode": (I32, [I32]),
     "axc_row_engine_fix_capacity": (U32, [U32]),
     "axc_extract_outgoing_spikes_noalloc": (I32, [P, P, P, U32, U32, U32, P, P, P]),
+    "axc_population_create": (I32, [P, U32, C.POINTER(P)]),
+    "axc_population_run": (I32, [P, U32, U32, U32, P]),
+    "axc_population_tune": (I32, [P, U32, U32, P, P, C.POINTER(C.c_float), U32]),
+    "axc_population_set_schedule": (I32, [P, P]),
+    "axc_population_counters": (I32, [P, C.POINTER(C.c_uint64)]),
+    "axc_population_destroy": (None, [P]),
+    "axc_population_fix_capacity": (U32, [U32]),
     "axc_brain_layout": (I32, [C.POINTER(AxcBrainSpec), C.POINTER(AxcBrainLayout)]),
     "axc_brain_generate": (I32, [C.POINTER(AxcBrainSpec), P, P, I32]),
     "axc_input_bitmask": (I32, [C.c_uint64, U32, U32, U32, P, U32, P]),

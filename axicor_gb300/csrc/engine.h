@@ -57,7 +57,7 @@ struct ShardScratch {
 constexpr uint32_t kFixCap = 1u << 22;  // deferred GSOP slots per tick before the rescan path
 
 // Row engine (row_engine.cuh, compiled in day_phase.cu).
-cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A);
+cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix = true);
 void rows_free(ShardScratch& s);
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream);
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream);

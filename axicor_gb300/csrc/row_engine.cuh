@@ -650,8 +650,8 @@ __global__ void k_rows_reset_lists(ShardCtl* ctl) {
 
 }  // namespace
 
-cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A) {
-  if (s.rows && s.rows->N >= N && s.rows->A >= A) return cudaSuccess;
+cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
+  if (s.rows && s.rows->N >= N && s.rows->A >= A && (s.rows->fix || !with_fix)) return cudaSuccess;
   rows_free(s);
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   size_t off = 0;
@@ -661,7 +661,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A) {
   const size_t o_m2 = off; off = al(off + ((size_t)A + 1) * 8);
   const size_t o_mult = off; off = al(off + (size_t)A * 4);
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
-  const size_t o_fix = off; off = al(off + (size_t)kFixCap * 4);
+  const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
   if (e != cudaSuccess) return e;
@@ -678,7 +678,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A) {
   r->mask2 = reinterpret_cast<uint2*>(b + o_m2);
   r->mult = reinterpret_cast<uint32_t*>(b + o_mult);
   r->eval = reinterpret_cast<uint32_t*>(b + o_eval);
-  r->fix = reinterpret_cast<uint32_t*>(b + o_fix);
+  r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   s.rows = r;
   return cudaSuccess;
 }

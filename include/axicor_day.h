@@ -363,6 +363,9 @@ int32_t axc_population_set_schedule(void* handle, const AxcPopSchedule* schedule
  * [4] GSOP slots, [5] evaluated neurons; plus [6] the error bits of all brains. */
 int32_t axc_population_counters(void* handle, uint64_t out[8]);
 void axc_population_destroy(void* handle);
+/* Capacity of the population's per-tick list of deferred GSOP slots (as
+ * axc_row_engine_fix_capacity, for tests of the rescan path). */
+uint32_t axc_population_fix_capacity(uint32_t cap);
 
 /* ---- Synthetic brain generator (host) ---------------------------------- */
 /* Neurons fill a dim_x*dim_y*dim_z voxel grid (x fastest, one per voxel);
