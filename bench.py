@@ -42,7 +42,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plain-1.5M", choices=sorted(CONFIGS))
+    ap.add_argument("--workload", default="plain-1.5M", choices=sorted(CONFIGS) + ["population-512"])
+    ap.add_argument("--pop-brains", type=int, default=512)
+    ap.add_argument("--pop-ticks", type=int, default=2000)
     ap.add_argument("--ticks-per-step", type=int, default=100)
     ap.add_argument("--outputs", type=int, default=4096)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
@@ -387,8 +389,92 @@ def run_reference(args, dist: Dist) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_population(args) -> None:
+    """512 independent brains (neurons log-uniform in [1k,100k], slots in {32,64,96,128}, per-brain
+    threshold / leak shift / GSOP / input rate), 2,000 ticks each: the population engine against the same
+    brains stepped one after another through the batch entry point; every final state compared."""
+    import hashlib
+    import torch
+    import __graft_entry__ as G
+    G.build()
+    from axicor_gb300 import _native as N
+    from axicor_gb300 import population as Pop
+    from axicor_gb300 import workloads as W
+    lib = N.lib()
+    lib.gpu_set_device(0)
+    count, ticks, tpg = args.pop_brains, args.pop_ticks, args.ticks_per_step
+    t0 = time.perf_counter()
+    ws = W.population(count=count, ticks=ticks)
+    brains = [Pop.Brain(w, ticks) for w in ws]
+    synapses = sum(b.synapses for b in brains)
+    neurons = sum(b.lay.num_neurons for b in brains)
+    setup_s = time.perf_counter() - t0
+
+    def digest(b):
+        h = hashlib.sha256()
+        h.update(b.vram.download_state().tobytes())
+        h.update(b.vram.download_heads().tobytes())
+        return h.hexdigest()
+
+    pop = Pop.Population(brains)
+    sc, cand_ms = pop.tune(0, 2, None)
+    pop.run(0, tpg, tpg)                       # captures the graph (untimed)
+    for b in brains:
+        b.reset()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(0)
+    clocks.start()
+    e0.record()
+    pop.run(0, ticks, tpg)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    pop_s = e0.elapsed_time(e1) / 1e3
+    ctr = pop.counters()
+    pop_digest = [digest(b) for b in brains]
+    pop.close()
+    # sequential: each brain alone through the batch entry point (graphs captured untimed first)
+    for b in brains:
+        b.run_alone(0, tpg, batch=tpg)
+        b.reset()
+    torch.cuda.synchronize()
+    s0 = time.perf_counter()
+    for b in brains:
+        b.run_alone(0, ticks, batch=tpg)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - s0
+    same = sum(1 for b, d in zip(brains, pop_digest) if digest(b) == d)
+    events = synapses * ticks
+    line = {
+        "metric": "synaptic_events_per_s", "value": events / pop_s, "unit": "events/s", "n_gpus": 1, "steps": 1,
+        "warmup": 0, "ms_per_step": pop_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic (seeded generator, inputs resident in HBM)",
+        "config": {"workload": f"population-{count}", "brains": count, "neurons": neurons, "synapses": synapses,
+                   "ticks": ticks, "ticks_per_graph": tpg,
+                   "schedule": {"lanes_per_neuron": sc.lanes_per_neuron,
+                                "update_blocks_per_sm": sc.update_blocks_per_sm,
+                                "aux_blocks_per_sm": sc.aux_blocks_per_sm}},
+        "tuner_candidate_ms": cand_ms,
+        "sequential": {"value": events / seq_s, "unit": "events/s", "seconds": seq_s,
+                       "how": "each brain alone through axc_step_day_phase_batch, batches of "
+                              f"{tpg} ticks, one after another"},
+        "speedup_vs_sequential": seq_s / pop_s,
+        "bitexact_brains": f"{same}/{count}",
+        "per_tick": {"evaluated_slots": int(ctr[1]) / ticks, "spikes": int(ctr[3]) / ticks},
+        "errors": int(ctr[6]),
+        "clocks": clk, "setup_s": setup_s,
+    }
+    print(json.dumps(line), flush=True)
+    for b in brains:
+        b.free()
+
+
 def main():
     args = parse()
+    if args.workload.startswith("population"):
+        run_population(args)
+        return
     dist = Dist(args.gpus)
     try:
         if args.impl == "reference":

@@ -24,10 +24,10 @@ def mixed_population(count=10, seed=3):
     ws[1].lut[0]["homeostasis_penalty"] = 30
     ws[2].lut[1]["spontaneous_firing_period_ticks"] = 5
     ws[3].lut[0]["signal_propagation_length"] = 6          # mixed lengths: exact head tests
-    ws[4].dopamine = 120
+    ws[-1].dopamine = 120
     for v in (0, 1):
-        ws[4].lut[v]["d1_affinity"] = 60
-        ws[4].lut[v]["d2_affinity"] = 90
+        ws[-1].lut[v]["d1_affinity"] = 60
+        ws[-1].lut[v]["d2_affinity"] = 90
     return ws
 
 
