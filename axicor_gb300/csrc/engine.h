@@ -34,6 +34,7 @@ struct RowCache {
   uint32_t* mult = nullptr; // [A] number of somas that own the axon
   uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
+  uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each
 };
 
 // Per-shard scratch owned by the engine, next to the reference-visible

@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint2* __restrict__ mask2, const uint32_t* __restrict__ mult,
                                                        uint8_t* __restrict__ flags, uint8_t* __restrict__ timers,
                                                        uint32_t N, uint32_t* __restrict__ eval,
-                                                       ShardCtl* __restrict__ ctl, uint32_t raise_err) {
+                                                       ShardCtl* __restrict__ ctl, uint32_t raise_err,
+                                                       uint32_t* __restrict__ lit_bits) {
   __shared__ uint32_t s_pmax, s_base;
   __shared__ int s_inc;
   __shared__ uint32_t s_warp[8];
@@ -261,6 +262,7 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
   }
   __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool lit = false;
   if (i < A) {
     uint4* p = reinterpret_cast<uint4*>(heads + i);
     const uint4 x = p[0], y = p[1];
@@ -280,7 +282,15 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
       if (h[j] != AXC_AXON_SENTINEL) h[j] += v_seg;
     p[0] = make_uint4(h[0], h[1], h[2], h[3]);
     p[1] = make_uint4(h[4], h[5], h[6], h[7]);
-    mask2[i] = split_masks(h, s_pmax, mult[i]);
+    const uint2 m = split_masks(h, s_pmax, mult[i]);
+    mask2[i] = m;
+    // fully lit: heads 0..6 hit every segment 1..30 and at most one soma owns
+    // the axon, so for those segments the hit is 1 and one push cannot change it
+    lit = (m.x & 0x7FFFFFFEu) == 0x7FFFFFFEu && !(m.y >> 31);
+  }
+  if (lit_bits) {
+    const uint32_t lb = __ballot_sync(kFull, lit);
+    if ((threadIdx.x & 31) == 0 && i < A) lit_bits[i >> 5] = lb;
   }
   bool ev = false;
   if (i < N) {
@@ -345,22 +355,29 @@ __device__ __noinline__ int gsop_general(const BurstHeads8* heads, const uint2* 
   return 0;
 }
 
-__global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A,
-                                                        const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
-                                                        const uint16_t* __restrict__ cnt,
-                                                        const uint2* __restrict__ mask2,
-                                                        const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend,
-                                                        uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
-                                                        uint32_t k, uint32_t fix_cap) {
+// LIT: 1024-thread blocks (one per SM) that first copy the prologue's
+// fully-lit bitmap (one bit per axon) into shared memory; slots whose axon is
+// fully lit need no mask gather from L2.
+template <bool LIT>
+__global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
+    k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A, const uint32_t* __restrict__ rt,
+                  int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
+                  const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
+                  ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits) {
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];   // GSOP (potentiation, depression) per variant and inertia rank
   __shared__ uint32_t s_pmax;
+  extern __shared__ uint32_t s_lit[];
   lut_to_smem(lut);
   if (threadIdx.x == 0) s_pmax = lut_pmax();
+  if (LIT) {
+    const uint32_t words = (A >> 5) + 1;
+    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) s_lit[w] = __ldg(lit_bits + w);
+  }
   __syncthreads();
   const uint32_t tick = ctl->tick_base + k;
   const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
-  {
+  if (threadIdx.x < 256) {
     // a spiker's flags after the update are type | 0b101, so its burst multiplier
     // is 2 (physics.cu:255, 271-273, 290-291); physics.cu:336-349 for each rank
     const uint32_t v = threadIdx.x >> 4, r = threadIdx.x & 15;
@@ -415,14 +432,22 @@ __global__ void __launch_bounds__(256, 4) k_rows_update(ShardVramPtrs P, uint32_
       for (int j = 0; j < 4; j++) {
         const uint32_t q0 = 32u * j + 4u * g8;
         uint2 m[4];
+        bool lit[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          const uint32_t ax = (word_of(T[j], i) & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
-          m[i] = (q0 + i < c) ? __ldg(mask2 + ax) : make_uint2(0, 0);
+          const uint32_t t = word_of(T[j], i);
+          const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
+          lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < 30u && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
+          m[i] = (q0 + i < c && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
         }
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           if (q0 + i >= c) continue;
+          if (LIT && lit[i]) {                      // segment 1..30 of a fully lit axon: hit, fast GSOP
+            i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+            hitb |= 1u << (4 * j + i);
+            continue;
+          }
           const uint32_t t = word_of(T[j], i);
           const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
           const uint32_t sh = min(s, 31u);
@@ -662,6 +687,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_mult = off; off = al(off + (size_t)A * 4);
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
+  const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
   if (e != cudaSuccess) return e;
@@ -679,6 +705,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->mult = reinterpret_cast<uint32_t*>(b + o_mult);
   r->eval = reinterpret_cast<uint32_t*>(b + o_eval);
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
+  r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
   s.rows = r;
   return cudaSuccess;
 }
@@ -705,6 +732,23 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
 
 // One tick of the row engine (batch mode): prologue, update (+GSOP), fix-up, push.
 // ev (optional) gets the stage boundaries 2..5 recorded (GSOP is part of update).
+// Largest fully-lit bitmap the update kernel stages in shared memory (the
+// 1024-thread variant also uses ~3.4 KB of static shared memory).
+static size_t lit_smem_limit() {
+  static size_t limit = [] {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t lim = optin > 8192 ? (size_t)optin - 8192 : 0;
+    if (cudaFuncSetAttribute(k_rows_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) != cudaSuccess) {
+      cudaGetLastError();
+      lim = 0;
+    }
+    return lim;
+  }();
+  return limit;
+}
+
 cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
                              cudaEvent_t* ev, bool have_incoming) {
   RowCache& r = *s.rows;
@@ -718,10 +762,16 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
     k_rows_prologue<<<(G + 255) / 256, 256, 0, stream>>>(
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
-        raise);
+        raise, r.lit);
   if (ev) cudaEventRecord(ev[2], stream);
-  k_rows_update<<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, a.k,
-                                             min(a.fix_cap, kFixCap));
+  const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
+  if (lit_bytes <= lit_smem_limit()) {
+    k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                        s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit);
+  } else {
+    k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                      s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit);
+  }
   if (ev) cudaEventRecord(ev[3], stream);
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
