@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
     bool bad = false;
+    uint32_t smx = 0;
     for (uint32_t q = lane; q < c; q += 32) {
       uint32_t t = s_t[q][j];
       // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
@@ -189,13 +190,18 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
         t = (t & ~AXC_TARGET_AXON_MASK) | (A + 1u);
         bad = true;
       }
+      smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
       rt[(size_t)n * kRowStride + q] = t;
       rw[(size_t)n * kRowStride + q] = s_w[q][j];
     }
     bad = __any_sync(kFull, bad);
+    smx = __reduce_max_sync(kFull, smx);
     if (lane == 0) {
       cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
-      if (c) atomicMax(&ctl->row_smax, c);
+      if (c) {
+        atomicMax(&ctl->row_smax, c);
+        atomicMax(&ctl->seg_max, smx);
+      }
     }
   }
 }
@@ -207,6 +213,7 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
   if (n == 0) {
     mask2[A] = make_uint2(0u, 0x80000000u);   // dummy entry of invalid targets: no hit, exact path
     ctl->row_smax = 0;
+    ctl->seg_max = 0;
   }
   if (n >= N) return;
   const uint32_t a = s2a[n];
@@ -249,11 +256,13 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint32_t N, uint32_t* __restrict__ eval,
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err,
                                                        uint32_t* __restrict__ lit_bits) {
-  __shared__ uint32_t s_pmax, s_base;
+  __shared__ uint32_t s_pmax, s_base, s_need;
   __shared__ int s_inc;
   __shared__ uint32_t s_warp[8];
   if (threadIdx.x == 0) {
     s_pmax = lut_pmax();
+    const uint32_t hi = min(ctl->seg_max, 30u);   // segments 1..hi are the ones the batch's slots use
+    s_need = hi ? (((2u << hi) - 1u) & ~1u) : 0xFFFFFFFFu;
     s_inc = batch_counts && batch_counts[k] > 0;
     if (blockIdx.x == 0) {
       ctl->ctr[0] += 1;
@@ -284,9 +293,10 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
     p[1] = make_uint4(h[4], h[5], h[6], h[7]);
     const uint2 m = split_masks(h, s_pmax, mult[i]);
     mask2[i] = m;
-    // fully lit: heads 0..6 hit every segment 1..30 and at most one soma owns
-    // the axon, so for those segments the hit is 1 and one push cannot change it
-    lit = (m.x & 0x7FFFFFFEu) == 0x7FFFFFFEu && !(m.y >> 31);
+    // fully lit: heads 0..6 hit every segment 1..seg_max the batch uses and at
+    // most one soma owns the axon, so for those segments the hit is 1 and one
+    // push cannot change it
+    lit = (m.x & s_need) == s_need && !(m.y >> 31);
   }
   if (lit_bits) {
     const uint32_t lb = __ballot_sync(kFull, lit);
@@ -388,6 +398,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   __syncthreads();
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t smax = ctl->row_smax;   // longest row of the shard: rows are loaded up to here
+  const uint32_t seg_hi = min(ctl->seg_max, 30u);   // lit bits cover segments 1..seg_hi
   const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -437,7 +448,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
         for (int i = 0; i < 4; i++) {
           const uint32_t t = word_of(T[j], i);
           const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
-          lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < 30u && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
+          lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
           m[i] = (q0 + i < c && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
         }
 #pragma unroll
