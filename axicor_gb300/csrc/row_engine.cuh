@@ -438,41 +438,43 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       const bool gfast = exact && prop <= 16u;
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
       int32_t i_in = 0;
-      uint32_t hitb = 0, slowb = 0, liveb = 0;   // bit 4j+i
+      uint32_t hitb = 0, slowb = 0;   // bit 4j+i
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const uint32_t q0 = 32u * j + 4u * g8;
-        const uint32_t nl = c > q0 ? min(c - q0, 4u) : 0u;   // live slots of this chunk
-        liveb |= ((1u << nl) - 1u) << (4 * j);
         uint2 m[4];
         bool lit[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           const uint32_t t = word_of(T[j], i);
-          const bool live = (uint32_t)i < nl;
-          const uint32_t ax = live ? (t & AXC_TARGET_AXON_MASK) - 1u : 0u;   // invalid ids were redirected to A
-          lit[i] = LIT && live && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi &&
-                   ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
-          m[i] = (live && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
+          const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
+          lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
+          m[i] = (q0 + i < c && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
         }
 #pragma unroll
         for (int i = 0; i < 4; i++) {
+          if (q0 + i >= c) continue;
+          if (LIT && lit[i]) {                      // segment 1..30 of a fully lit axon: hit, fast GSOP
+            i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+            hitb |= 1u << (4 * j + i);
+            continue;
+          }
           const uint32_t t = word_of(T[j], i);
           const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
           const uint32_t sh = min(s, 31u);
           const uint32_t bx = (m[i].x >> sh) & 1u, by = (m[i].y >> sh) & 1u;
-          // bit 31 (s >= 31) means "may hit": tested exactly below (rare)
-          bool hit = lit[i] || (bx | by);
-          if (!lit[i] && hit && (s >= 31u || !exact))
+          bool hit = (bx | by) != 0u;              // bit 31 (s >= 31): "may hit", tested below
+          if (hit && (s >= 31u || !exact))
             hit = hit_exact(P.axon_heads, A, (t & AXC_TARGET_AXON_MASK) - 1u, s, prop);
-          i_in = wadd(i_in, hit ? (int32_t)half_of(W[j], i) : 0);
-          hitb |= (uint32_t)hit << (4 * j + i);
+          if (hit) {
+            i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+            hitb |= 1u << (4 * j + i);
+          }
           // fast GSOP: hit decides, and one same-tick push could not change it
-          const bool fast = lit[i] || (gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u)));
-          slowb |= (uint32_t)!fast << (4 * j + i);
+          const bool fast = gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u));
+          slowb |= fast ? 0u : (1u << (4 * j + i));
         }
       }
-      slowb &= liveb;
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
@@ -520,47 +522,41 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       }
       // GSOP on the row in registers (physics.cu:281-373)
       if (spike) {
-        // fast slots: cooling shift 0, delta = +potentiation or -depression of the weight's rank
 #pragma unroll
         for (int j = 0; j < 4; j++) {
+          const uint32_t q0 = 32u * j + 4u * g8;
+          if (q0 >= c) continue;
           uint2 wj = W[j];
 #pragma unroll
           for (int i = 0; i < 4; i++) {
             const uint32_t b = 1u << (4 * j + i);
+            if (q0 + i >= c) continue;
             const int16_t w16 = half_of(wj, i);
-            const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
-            const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
-            int32_t na = aw + ((hitb & b) ? e.x : -e.y);
-            na = min(max(na, 0), 32767);
-            const bool apply = (liveb & ~slowb & b) != 0u;
-            set_half(wj, i, apply ? (int16_t)(w16 < 0 ? -na : na) : w16);
+            if (!(slowb & b)) {
+              // cooling shift 0: delta = +potentiation or -depression of the weight's rank
+              const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+              const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
+              int32_t na = aw + ((hitb & b) ? e.x : -e.y);
+              na = min(max(na, 0), 32767);
+              set_half(wj, i, (int16_t)(w16 < 0 ? -na : na));
+              gdone++;
+              continue;
+            }
+            const uint32_t t = __ldg(trow + 32 * j + i);
+            int16_t nw = w16;
+            const int r = gsop_general(P.axon_heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u,
+                                       t >> AXC_TARGET_SEG_SHIFT, p, flags, dopamine, &nw);
+            if (r == 2) continue;
+            gdone++;
+            if (r == 1) {
+              const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+              if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
+              else ctl->fix_overflow = 1u;
+              continue;
+            }
+            set_half(wj, i, nw);
           }
-          if (wj.x != W[j].x || wj.y != W[j].y) {
-            *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
-            W[j] = wj;
-          }
-        }
-        gdone += __popc(liveb & ~slowb);
-        // slow slots (rare): exact distances, or deferred to the fix-up stage
-        uint32_t rest = slowb;
-        while (rest) {
-          const int bit = __ffs(rest) - 1;
-          rest &= rest - 1;
-          const int j = bit >> 2, i = bit & 3;
-          const uint32_t q = 32u * j + 4u * g8 + i;
-          const uint32_t t = __ldg(trow + 32 * j + i);
-          int16_t w16 = wrow[32 * j + i];
-          const int r = gsop_general(P.axon_heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u,
-                                     t >> AXC_TARGET_SEG_SHIFT, p, flags, dopamine, &w16);
-          if (r == 2) continue;
-          gdone++;
-          if (r == 1) {
-            const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
-            if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q);
-            else ctl->fix_overflow = 1u;
-            continue;
-          }
-          wrow[32 * j + i] = w16;
+          if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
         }
       }
     }
