@@ -97,6 +97,17 @@ class AxcPopSchedule(C.Structure):
                 ("aux_blocks_per_sm", C.c_uint32)]
 
 
+class AxcLearnedDesc(C.Structure):
+    _fields_ = [
+        ("vram", ShardVramPtrs),
+        ("padded_n", C.c_uint32), ("total_axons", C.c_uint32),
+        ("virtual_offset", C.c_uint32), ("num_virtual", C.c_uint32),
+        ("d_input_bitmask", C.c_void_p), ("words_per_tick", C.c_uint32), ("bitmask_ticks", C.c_uint32),
+        ("v_seg", C.c_uint32), ("dopamine", C.c_int32), ("tick_base", C.c_uint32),
+        ("sample_capacity", C.c_uint32),
+    ]
+
+
 class AxcBrainSpec(C.Structure):
     _fields_ = [
         ("dim_x", C.c_uint32), ("dim_y", C.c_uint32), ("dim_z", C.c_uint32),
@@ -174,6 +185,21 @@ SIGNATURES: dict[str, tuple] = {
     "axc_population_counters": (I32, [P, C.POINTER(C.c_uint64)]),
     "axc_population_destroy": (None, [P]),
     "axc_population_fix_capacity": (U32, [U32]),
+    "axc_learned_create": (I32, [C.POINTER(AxcLearnedDesc), C.POINTER(P)]),
+    "axc_learned_refresh": (I32, [P, P]),
+    "axc_learned_set_policy": (I32, [P, I32, C.c_float, C.c_float, U32]),
+    "axc_learned_collect": (I32, [P, U32, U32, U32]),
+    "axc_learned_run": (I32, [P, U32, U32, U32, P]),
+    "axc_learned_train": (I32, [P, U32, U32, C.c_float, C.c_uint64, C.POINTER(C.c_float),
+                                C.POINTER(C.c_float), P]),
+    "axc_learned_params": (I32, [P, P, P]),
+    "axc_learned_samples": (I32, [P, U32, U32, P, P]),
+    "axc_learned_stats": (I32, [P, C.POINTER(C.c_uint64)]),
+    "axc_learned_reset_stats": (I32, [P]),
+    "axc_learned_destroy": (None, [P]),
+    "axc_mlp_param_count": (U32, []),
+    "axc_mlp_loss_grad": (I32, [P, P, P, U32, P, P, P]),
+    "axc_mlp_predict": (I32, [P, P, U32, P, P]),
     "axc_brain_layout": (I32, [C.POINTER(AxcBrainSpec), C.POINTER(AxcBrainLayout)]),
     "axc_brain_generate": (I32, [C.POINTER(AxcBrainSpec), P, P, I32]),
     "axc_input_bitmask": (I32, [C.c_uint64, U32, U32, U32, P, U32, P]),

@@ -633,3 +633,4 @@ cudaError_t launch_spike_list_sorted(const ShardVramPtrs& v, uint32_t padded_n, 
 }  // namespace axc
 
 #include "population.cuh"
+#include "learned.cuh"

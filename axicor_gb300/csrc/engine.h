@@ -19,7 +19,7 @@ struct ShardCtl {
   uint32_t eval_count[2]; // row engine: non-refractory neurons listed in tick k (slot k & 1)
   uint32_t row_smax;      // row engine: longest row (slots before the first empty) of the batch
   uint32_t seg_max;       // row engine: largest segment of a live slot in the batch
-  uint32_t pad[2];
+  unsigned long long row_sum;  // row engine: checksum of the batch's targets (slot order)
   unsigned long long ctr[8];  // statistics, see axc_shard_counters
 };
 

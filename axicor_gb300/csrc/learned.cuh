@@ -1,0 +1,1246 @@
+// learned.cuh — the learned-schedule engine (compiled as part of day_phase.cu,
+// after row_engine.cuh, whose kernels it shares).
+//
+// A small MLP (64 -> 128 -> 1, BF16 weights, FP32 accumulation) predicts, per
+// tile of 1024 axons, how many synapses will be active on the next tick (the
+// fan-out of the tile's axons whose heads cover at least one segment).  Before
+// each tick the plan kernel turns the predictions into a schedule:
+//
+//   dense   the row engine's update pass (every evaluated neuron reads its
+//           whole dendrite row);
+//   sparse  an axon-driven gather: the prologue compacts the active axons into
+//           per-tile segments sized from the prediction, k_learn_scatter walks
+//           an inverted index (axon -> dendrite slots) and adds the weights of
+//           hit slots into the evaluated neurons' input current, k_learn_update
+//           runs GLIF from that current, and k_learn_gsop applies GSOP to the
+//           spikers' rows with the row engine's own slot code.
+//
+// A tile whose actual activity exceeds its pre-sized segment sets the overflow
+// flag in the prologue; the dense kernels then run the tick and the sparse
+// ones return at once, so a misprediction costs time and never changes a
+// result.  The dendrite input current is a wrapping int32 sum, so the order in
+// which the scatter adds weights does not matter: both schedules give the
+// plain path's state bit for bit.
+//
+// Training data come from the simulator: while collecting, the features
+// kernel records (features of tick t-1, active-synapse fraction of tick t)
+// per tile.  Training runs on the GPU with the kernels at the end of this
+// file: forward + backward per block over a slice of the minibatch, a
+// fixed-order reduction of the block partials and an Adam step that also
+// refreshes the BF16 copy of the weights.
+
+#include <cuda_bf16.h>
+
+namespace axc {
+namespace {
+
+constexpr uint32_t kTileN = 1024;
+constexpr uint32_t kFeat = 64, kHid = 128;
+constexpr uint32_t kOffB1 = kHid * kFeat, kOffW2 = kOffB1 + kHid, kOffB2 = kOffW2 + kHid;
+constexpr uint32_t kParams = kOffB2 + 1;   // W1[128][64], b1[128], w2[128], b2
+constexpr uint32_t kHistCh = 4;            // spikes, active synapses, heads in flight, evaluated
+constexpr uint32_t kHistLen = 8;
+constexpr uint32_t kHistF = kHistCh * kHistLen + 1;   // + the tile's next-tick evaluated count
+constexpr uint32_t kGradPer = 16;          // samples per block of the gradient kernel
+
+// LearnCtl.stat[]
+enum : int {
+  kStTicks = 0,        // ticks run by the learned engine
+  kStSparse = 1,       // ticks that ran sparse
+  kStOverflow = 2,     // sparse ticks re-run dense (a tile outgrew its segment)
+  kStMismatch = 3,     // ticks whose schedule differs from the one exact counts pick
+  kStAbsErr = 4,       // sum over tiles of |predicted - actual| active synapses
+  kStActual = 5,       // sum over tiles of actual active synapses
+  kStJudged = 6,       // ticks counted in kStMismatch / kStAbsErr
+  kStSparsePicked = 7, // ticks planned sparse
+  kStStale = 8,        // ticks forced dense because the targets changed
+};
+
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+// One hidden unit u of the MLP on the BF16-rounded input xs (shared memory):
+// returns the pre-activation (FP32, k = 0..63 in order).
+__device__ __forceinline__ float mlp_unit(const __nv_bfloat16* __restrict__ wb, uint32_t u, const float* xs) {
+  const uint4* row = reinterpret_cast<const uint4*>(wb + u * kFeat);
+  float a = __bfloat162float(wb[kOffB1 + u]);
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const uint4 q = __ldg(row + c);
+    const uint32_t wv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const float lo = __uint_as_float(wv[e] << 16), hi = __uint_as_float(wv[e] & 0xFFFF0000u);
+      a = fmaf(lo, xs[c * 8 + 2 * e], a);
+      a = fmaf(hi, xs[c * 8 + 2 * e + 1], a);
+    }
+  }
+  return a;
+}
+
+// Output of the MLP for the input in xs, computed by a 128-thread block
+// (thread u = hidden unit u); a fixed reduction order, so deterministic.
+__device__ __forceinline__ float mlp_block_forward(const __nv_bfloat16* __restrict__ wb, const float* xs, float* red,
+                                                   float* a_out, float* hb_out) {
+  const uint32_t u = threadIdx.x;
+  const float a = mlp_unit(wb, u, xs);
+  const float hb = bf16r(a > 0.f ? a : 0.f);
+  float part = __fmul_rn(__bfloat162float(wb[kOffW2 + u]), hb);
+  part = warp_sum_f(part);
+  __syncthreads();
+  if ((u & 31) == 0) red[u >> 5] = part;
+  __syncthreads();
+  const float y = __fadd_rn(__fadd_rn(__fadd_rn(red[0], red[1]), __fadd_rn(red[2], red[3])),
+                            __bfloat162float(wb[kOffB2]));
+  if (a_out) *a_out = a;
+  if (hb_out) *hb_out = hb;
+  return y;
+}
+
+// Block-wide exclusive scan of cnt[0..n) (1024 threads, n <= 1024 * 64) into
+// out[0..n], out[n] = total.
+__device__ void block_scan_1024(const uint32_t* cnt, uint32_t* out, uint32_t n) {
+  __shared__ uint32_t s[1024];
+  const uint32_t per = (n + 1023) / 1024;
+  const uint32_t b = threadIdx.x * per;
+  uint32_t t = 0;
+  for (uint32_t q = 0; q < per; q++)
+    if (b + q < n) t += cnt[b + q];
+  s[threadIdx.x] = t;
+  __syncthreads();
+  for (uint32_t o = 1; o < 1024; o <<= 1) {
+    const uint32_t x = threadIdx.x >= o ? s[threadIdx.x - o] : 0u;
+    __syncthreads();
+    s[threadIdx.x] += x;
+    __syncthreads();
+  }
+  uint32_t run = s[threadIdx.x] - t;
+  for (uint32_t q = 0; q < per; q++)
+    if (b + q < n) {
+      const uint32_t c = cnt[b + q];
+      out[b + q] = run;
+      run += c;
+    }
+  if (threadIdx.x == 1023) out[n] = s[1023];
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// per tick 0: the schedule.  One block of 1024 threads.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __restrict__ pred,
+                                                     const uint32_t* __restrict__ fan,
+                                                     const uint32_t* __restrict__ axn, uint32_t* __restrict__ cap,
+                                                     uint32_t* __restrict__ seg, uint32_t* __restrict__ entries,
+                                                     const uint32_t* __restrict__ bits, uint32_t words, uint32_t nv,
+                                                     const ShardCtl* __restrict__ sc, uint32_t features_on) {
+  LearnCtl& c = *L.ctl;
+  const uint32_t T = c.T;
+  __shared__ float s_pf[32];
+  __shared__ unsigned long long s_y[32];
+  __shared__ uint32_t s_in[32];
+  __shared__ uint32_t s_sparse;
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // the previous tick, judged with exact counts: its total active synapses
+  // (still in yacc) and its evaluated slots
+  unsigned long long y = 0;
+  float pf = 0.f;
+  for (uint32_t j = threadIdx.x; j < T; j += 1024) {
+    y += L.yacc[j];
+    pf += fmaxf(pred[j], 0.f) * (float)fan[j];
+  }
+  uint32_t ib = 0;
+  for (uint32_t q = threadIdx.x; q < words; q += 1024) {
+    uint32_t x = bits ? bits[q] : 0u;
+    if (32u * q + 32u > nv) x &= (32u * q >= nv) ? 0u : ((1u << (nv - 32u * q)) - 1u);
+    ib += __popc(x);
+  }
+  y = warp_sum(y);
+  pf = warp_sum_f(pf);
+  ib = warp_sum(ib);
+  if (lane == 0) { s_y[w] = y; s_pf[w] = pf; s_in[w] = ib; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long ty = 0;
+    float tp = 0.f;
+    uint32_t ti = 0;
+    for (int q = 0; q < 32; q++) { ty += s_y[q]; tp += s_pf[q]; ti += s_in[q]; }
+    // the previous tick, judged with exact counts when the predictor chose its schedule
+    if (c.prev_learned) {
+      const bool best_sparse = c.ratio * (float)ty < (float)c.eval_now;
+      if (best_sparse != (c.prev_mode == 1u)) c.stat[kStMismatch]++;
+      c.stat[kStJudged]++;
+    }
+    if (c.feat_done) {       // the features kernel completed the previous tick
+      if (c.collect && c.ticks_seen >= 1 && (c.ticks_seen % c.sample_every) == 0 && c.samples + T <= c.sample_cap)
+        c.samples += T;
+      c.ticks_seen++;
+      c.feat_done = 0;
+    } else {
+      c.ticks_seen = 0;      // the feature history restarts
+    }
+    for (int q = 8; q > 0; q--) c.inrate[q] = c.inrate[q - 1];
+    c.inrate[0] = nv ? (float)ti / (float)nv : 0.f;
+    c.stale = (sc->row_sum != c.row_sum) ? 1u : 0u;
+    const bool learned = features_on && c.policy < 0 && c.ticks_seen > 0 && !c.stale;
+    bool sparse;
+    if (c.stale) sparse = false;
+    else if (c.policy == 1) sparse = true;
+    else sparse = learned && c.ratio * tp < (float)c.eval_next;
+    if (c.stale) c.stat[kStStale]++;
+    c.stat[kStTicks]++;
+    if (sparse) c.stat[kStSparsePicked]++;
+    c.prev_learned = learned ? 1u : 0u;
+    c.pred_total = tp;
+    c.eval_now = c.eval_next;
+    c.eval_next = 0;
+    c.mode = sparse ? 1u : 0u;
+    c.prev_mode = c.mode;
+    c.overflow = 0;
+    c.spk_count = 0;
+    s_sparse = sparse ? 1u : 0u;
+  }
+  __syncthreads();
+  const bool sparse = s_sparse != 0u;
+  const bool exact = c.policy == 1;
+  for (uint32_t j = threadIdx.x; j < T; j += 1024) {
+    uint32_t cp = 0;
+    if (sparse) {
+      if (exact) {
+        cp = fan[j];
+      } else {
+        const float want = fmaxf(pred[j], 0.f) * (float)fan[j] * (1.f + c.margin) + (float)c.slack;
+        cp = want >= (float)fan[j] ? fan[j] : (uint32_t)want;
+      }
+    }
+    cap[j] = cp;
+    entries[j] = min(cp, axn[j]);
+    L.yacc[j] = 0;
+    L.bacc[j] = 0;
+    L.fill[j] = 0;
+  }
+  __syncthreads();
+  block_scan_1024(entries, seg, T);
+}
+
+// ---------------------------------------------------------------------------
+// per tick 2s: the sparse gather.  A warp per active axon walks its slots in
+// the inverted index; hit slots of evaluated neurons add their weight to the
+// neuron's input current (wrapping int32, order-independent).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, const uint32_t* __restrict__ inv,
+                                                       const uint8_t* __restrict__ inv_seg,
+                                                       const uint2* __restrict__ mask2,
+                                                       const int16_t* __restrict__ rw,
+                                                       const uint8_t* __restrict__ flags,
+                                                       const BurstHeads8* __restrict__ heads, uint32_t A,
+                                                       int32_t* __restrict__ acc, ShardCtl* __restrict__ sc) {
+  LearnCtl& c = *L.ctl;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && c.mode == 1u) c.stat[c.overflow ? kStOverflow : kStSparse]++;
+  if (c.mode != 1u || c.overflow) return;
+  __shared__ uint32_t s_prop[16];
+  __shared__ uint32_t s_pmax;
+  if (threadIdx.x < 16) s_prop[threadIdx.x] = VARIANT_LUT[threadIdx.x].signal_propagation_length;
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t total = L.seg[T];
+  unsigned long long hits = 0;
+  for (uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < total; e += nwarps) {
+    // the tile whose segment holds position e
+    uint32_t lo = 0, hi = T;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(L.seg + mid) <= e) lo = mid; else hi = mid;
+    }
+    if (e - __ldg(L.seg + lo) >= L.fill[lo]) continue;
+    const uint32_t a = L.alist[e];
+    const uint2 m = __ldg(mask2 + a);
+    const uint32_t r0 = __ldg(L.inv_off + a), r1 = __ldg(L.inv_off + a + 1);
+    for (uint32_t r = r0 + lane; r < r1; r += 32) {
+      const uint32_t s = inv_seg[r];
+      const uint32_t sh = min(s, 31u);
+      if (!(((m.x | m.y) >> sh) & 1u)) continue;
+      const uint32_t slot = __ldg(inv + r);
+      const uint32_t n = slot / kRowStride;
+      if (!((__ldg(L.evbits + (n >> 5)) >> (n & 31u)) & 1u)) continue;
+      const uint32_t prop = s_prop[flags[n] >> 4];
+      bool hit = true;
+      if (s >= 31u || prop != s_pmax) hit = hit_exact(heads, A, a, s, prop);
+      if (hit) {
+        atomicAdd(acc + n, (int32_t)rw[slot]);
+        hits++;
+      }
+    }
+  }
+  block_count(0, hits, 0, &sc->ctr[1]);
+}
+
+// per tick 3s: GLIF of every evaluated neuron from the scattered current;
+// spikers push their axon and are listed for GSOP.
+__global__ void __launch_bounds__(256) k_learn_update(ShardVramPtrs P, LearnDev L, uint32_t A,
+                                                      const uint16_t* __restrict__ cnt,
+                                                      const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend,
+                                                      int32_t* __restrict__ acc, uint32_t* __restrict__ spk,
+                                                      ShardCtl* __restrict__ ctl, uint32_t k) {
+  LearnCtl& c = *L.ctl;
+  if (c.mode != 1u || c.overflow) return;
+  __shared__ VariantParameters lut[16];
+  lut_to_smem(lut);
+  __syncthreads();
+  const uint32_t tick = ctl->tick_base + k;
+  const uint32_t ecount = ctl->eval_count[k & 1];
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  unsigned long long ev_slots = 0, nspk = 0, nev = 0;
+  uint32_t err = 0;
+  for (uint32_t b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b0 < ecount; b0 += stride) {
+    const uint32_t i = b0 + lane;
+    const bool valid = i < ecount;
+    bool spike = false;
+    uint32_t n = 0;
+    if (valid) {
+      n = eval[i];
+      const uint8_t flags = P.soma_flags[n];
+      const uint32_t cw = cnt[n];
+      const int32_t i_in = acc[n];
+      acc[n] = 0;
+      const VariantParameters& p = lut[flags >> 4];
+      const GlifOut o = glif_step(p, P.soma_voltage[n], P.threshold_offset[n], i_in, tick, n);
+      spike = o.spike != 0;
+      P.soma_voltage[n] = o.v;
+      P.soma_flags[n] = (uint8_t)((flags & 0xF0) | (spike ? 0x05 : 0x00));
+      P.threshold_offset[n] = o.thr;
+      P.timers[n] = o.glif ? p.refractory_period : 0;
+      ev_slots += cw & 0xFFu;
+      nev++;
+      if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
+      if (spike) {
+        nspk++;
+        const uint32_t my_axon = P.soma_to_axon[n];
+        if (my_axon != AXC_NO_AXON) {
+          if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
+          else err |= AXC_ERR_SOMA_AXON;
+        }
+      }
+    }
+    const uint32_t ball = __ballot_sync(kFull, spike);
+    uint32_t base = 0;
+    if (lane == 0 && ball) base = atomicAdd(&c.spk_count, __popc(ball));
+    base = __shfl_sync(kFull, base, 0);
+    if (spike) spk[base + __popc(ball & ((1u << lane) - 1u))] = n;
+  }
+  const uint32_t err_any = __reduce_or_sync(kFull, err);
+  if (err_any && lane == 0) atomicOr(&ctl->err, err_any);
+  block_count(ev_slots, 0, nspk, &ctl->ctr[1]);
+  block_count(0, nev, 0, &ctl->ctr[4]);
+}
+
+// per tick 3s': GSOP of the sparse tick's spikers, 8 lanes per spiker, with
+// the row engine's slot classification and update (row_slots / row_gsop).
+__global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L, uint32_t A,
+                                                    const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
+                                                    const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
+                                                    const uint32_t* __restrict__ spk, uint32_t* __restrict__ fix,
+                                                    ShardCtl* __restrict__ ctl, uint32_t fix_cap) {
+  LearnCtl& c = *L.ctl;
+  if (c.mode != 1u || c.overflow) return;
+  __shared__ VariantParameters lut[16];
+  __shared__ int2 gtab[16][16];
+  __shared__ uint32_t s_pmax;
+  lut_to_smem(lut);
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
+  __syncthreads();
+  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
+  build_gtab(gtab, lut, dopamine);
+  __syncthreads();
+  const uint32_t count = c.spk_count;
+  const uint32_t smax = ctl->row_smax;
+  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  unsigned long long gdone = 0;
+  for (uint32_t base = wid * 4; base < count; base += nwarps * 4) {
+    const uint32_t idx = base + grp;
+    const bool valid = idx < count;
+    const uint32_t n = valid ? spk[idx] : 0u;
+    const uint8_t flags = P.soma_flags[n];
+    const uint32_t cw = valid ? cnt[n] : 0u;
+    const uint32_t* trow = rt + (size_t)n * kRowStride + 4u * g8;
+    int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
+    uint4 T[4];
+    uint2 W[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (valid && 32u * j + 4u * g8 < smax) {
+        T[j] = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
+        W[j] = *reinterpret_cast<const uint2*>(wrow + 32 * j);
+      } else {
+        T[j] = make_uint4(0, 0, 0, 0);
+        W[j] = make_uint2(0, 0);
+      }
+    }
+    const uint32_t cc = cw & 0xFFu;
+    const uint32_t var = flags >> 4;
+    const VariantParameters& p = lut[var];
+    const uint32_t prop = p.signal_propagation_length;
+    const bool exact = prop == s_pmax;
+    const bool gfast = exact && prop <= 16u;
+    uint32_t hitb, slowb;
+    (void)row_slots<false>(T, W, cc, g8, mask2, nullptr, 0u, exact, gfast, prop, P.axon_heads, A, hitb, slowb);
+    if (valid)
+      gdone += row_gsop(W, hitb, slowb, cc, g8, gtab, var, trow, wrow, P.axon_heads, mask2, A, p, flags, dopamine,
+                        ctl, fix, fix_cap, n);
+  }
+  block_count(gdone, 0, 0, &ctl->ctr[4]);
+}
+
+// ---------------------------------------------------------------------------
+// per tick 5: features of each tile after the tick, a recorded training pair
+// when collecting, and the prediction for the next tick.  A 128-thread block
+// per tile.
+//
+// Features (64): spikes, active-synapse fraction, heads in flight and
+// evaluated neurons of ticks t..t-7 (4 x 8); the input spike fraction of ticks
+// t..t-7 and t+1; the next tick's evaluated neurons and slots (exact: refractory
+// timers after the tick); the refractory histogram (timer 1, 2, 3, >= 4); the
+// tile's fan-out; a constant 1; zeros.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtrs P, uint32_t N,
+                                                        const uint16_t* __restrict__ cnt,
+                                                        const uint32_t* __restrict__ fan,
+                                                        const uint32_t* __restrict__ axn, float* __restrict__ hist,
+                                                        float* __restrict__ feat, float* __restrict__ pred,
+                                                        const __nv_bfloat16* __restrict__ wb, float* __restrict__ X,
+                                                        float* __restrict__ Y, const uint32_t* __restrict__ bits_next,
+                                                        uint32_t words, uint32_t nv) {
+  LearnCtl& c = *L.ctl;
+  const uint32_t j = blockIdx.x;
+  const uint32_t u = threadIdx.x, lane = u & 31, w = u >> 5;
+  __shared__ uint32_t s_cnt[8][4];
+  __shared__ float s_old[kHistF];
+  __shared__ float xb[kFeat];
+  __shared__ float red[4];
+  // 1. the tile's neurons after the tick
+  uint32_t spk = 0, nxt = 0, nslots = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, ib = 0;
+  const uint32_t n0 = j * kTileN;
+  for (uint32_t q = u; q < kTileN; q += 128) {
+    const uint32_t n = n0 + q;
+    if (n >= N) break;
+    const uint32_t tm = P.timers[n];
+    spk += P.soma_flags[n] & 1u;
+    if (tm == 0) { nxt++; nslots += cnt[n] & 0xFFu; }
+    t1 += tm == 1;
+    t2 += tm == 2;
+    t3 += tm == 3;
+    t4 += tm >= 4;
+  }
+  for (uint32_t q = u; q < words; q += 128) {
+    uint32_t x = bits_next ? bits_next[q] : 0u;
+    if (32u * q + 32u > nv) x &= (32u * q >= nv) ? 0u : ((1u << (nv - 32u * q)) - 1u);
+    ib += __popc(x);
+  }
+  const uint32_t vals[8] = {spk, nxt, nslots, t1, t2, t3, t4, ib};
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const uint32_t s = warp_sum(vals[q]);
+    if (lane == 0) s_cnt[q][w] = s;
+  }
+  if (u < kHistF) s_old[u] = hist[(size_t)j * kHistF + u];
+  __syncthreads();
+  uint32_t tot[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) tot[q] = s_cnt[q][0] + s_cnt[q][1] + s_cnt[q][2] + s_cnt[q][3];
+  const float fj = (float)max(fan[j], 1u);
+  const float aj = (float)max(axn[j], 1u);
+  const float y_now = (float)L.yacc[j] / fj;
+  // 2. training pair (features of the previous tick, this tick's target)
+  const bool seen = c.ticks_seen > 0;
+  if (seen && c.collect && (c.ticks_seen % c.sample_every) == 0 && c.samples + c.T <= c.sample_cap) {
+    const size_t row = (size_t)c.samples + j;
+    if (u < kFeat) X[row * kFeat + u] = feat[(size_t)j * kFeat + u];
+    if (u == 0) Y[row] = y_now;
+  }
+  if (u == 0 && seen && c.policy < 0) {
+    const float err = fabsf(fmaxf(pred[j], 0.f) - y_now) * fj;
+    atomicAdd(&c.stat[kStAbsErr], (unsigned long long)(err + 0.5f));
+    atomicAdd(&c.stat[kStActual], (unsigned long long)L.yacc[j]);
+  }
+  if (u == 0) atomicAdd(&c.eval_next, (unsigned long long)tot[2]);
+  // 3. history shift and the feature vector
+  const float cur[kHistCh] = {(float)tot[0] / (float)kTileN, y_now, (float)L.bacc[j] / (8.f * aj),
+                              s_old[kHistCh * kHistLen] / (float)kTileN};
+  float x = 0.f;
+  if (u < kHistCh * kHistLen) {
+    const uint32_t ch = u / kHistLen, i = u % kHistLen;
+    x = i == 0 ? cur[ch] : s_old[ch * kHistLen + i - 1];
+  } else if (u < 40) {
+    x = c.inrate[u - 32];
+  } else if (u == 40) {
+    x = nv ? (float)tot[7] / (float)nv : 0.f;
+  } else if (u == 41) {
+    x = (float)tot[1] / (float)kTileN;
+  } else if (u == 42) {
+    x = (float)tot[2] / (float)(kTileN * AXC_MAX_DENDRITES);
+  } else if (u >= 43 && u <= 46) {
+    x = (float)tot[3 + (u - 43)] / (float)kTileN;
+  } else if (u == 47) {
+    x = (float)fan[j] / (float)(kTileN * AXC_MAX_DENDRITES);
+  } else if (u == 48) {
+    x = 1.f;
+  }
+  __syncthreads();   // everyone has read s_old / feat before they are overwritten
+  if (u < kHistCh * kHistLen) hist[(size_t)j * kHistF + u] = x;
+  if (u == 0) hist[(size_t)j * kHistF + kHistCh * kHistLen] = (float)tot[1];
+  if (u < kFeat) {
+    xb[u] = bf16r(x);
+    feat[(size_t)j * kFeat + u] = x;
+  }
+  __syncthreads();
+  // 4. the prediction for the next tick
+  const float y = mlp_block_forward(wb, xb, red, nullptr, nullptr);
+  if (u == 0) pred[j] = y;
+  if (j == 0 && u == 0) c.feat_done = 1u;
+}
+
+// ---------------------------------------------------------------------------
+// Inverted index (axon -> dendrite slots), built from the rows.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_inv_count(const uint32_t* __restrict__ rt, const uint16_t* __restrict__ cnt,
+                                                   uint32_t N, uint32_t A, uint32_t* __restrict__ deg) {
+  const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (size_t)N * kRowStride) return;
+  const uint32_t n = (uint32_t)(r / kRowStride), q = (uint32_t)(r % kRowStride);
+  if (q >= (cnt[n] & 0xFFu)) return;
+  const uint32_t a = (rt[r] & AXC_TARGET_AXON_MASK) - 1u;
+  if (a < A) atomicAdd(deg + a, 1u);
+}
+
+__global__ void __launch_bounds__(256) k_inv_fill(const uint32_t* __restrict__ rt, const uint16_t* __restrict__ cnt,
+                                                  uint32_t N, uint32_t A, uint32_t* __restrict__ cursor,
+                                                  uint32_t* __restrict__ inv, uint8_t* __restrict__ inv_seg) {
+  const size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (size_t)N * kRowStride) return;
+  const uint32_t n = (uint32_t)(r / kRowStride), q = (uint32_t)(r % kRowStride);
+  if (q >= (cnt[n] & 0xFFu)) return;
+  const uint32_t t = rt[r];
+  const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
+  if (a >= A) return;
+  const uint32_t pos = atomicAdd(cursor + a, 1u);
+  inv[pos] = (uint32_t)r;
+  inv_seg[pos] = (uint8_t)(t >> AXC_TARGET_SEG_SHIFT);
+}
+
+// Exclusive scan of n <= 4096 * 4096 values: blocks of 4096, then the block sums.
+__global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                      uint32_t n, uint32_t* __restrict__ bsum) {
+  __shared__ uint32_t s[1024];
+  const uint32_t base = blockIdx.x * 4096u + threadIdx.x * 4u;
+  uint32_t v[4], t = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    v[i] = base + i < n ? in[base + i] : 0u;
+    t += v[i];
+  }
+  s[threadIdx.x] = t;
+  __syncthreads();
+  for (uint32_t o = 1; o < 1024; o <<= 1) {
+    const uint32_t x = threadIdx.x >= o ? s[threadIdx.x - o] : 0u;
+    __syncthreads();
+    s[threadIdx.x] += x;
+    __syncthreads();
+  }
+  uint32_t run = s[threadIdx.x] - t;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == 1023) bsum[blockIdx.x] = s[1023];
+}
+
+__global__ void __launch_bounds__(1024) k_scan_sums(uint32_t* __restrict__ bsum, uint32_t nb,
+                                                    uint32_t* __restrict__ out, uint32_t n) {
+  __shared__ uint32_t tmp[4097];
+  for (uint32_t i = threadIdx.x; i < nb; i += 1024) tmp[i] = bsum[i];
+  __syncthreads();
+  block_scan_1024(tmp, bsum, nb);   // bsum[0..nb] exclusive, bsum[nb] = total
+  if (threadIdx.x == 0) out[n] = bsum[nb];
+}
+
+__global__ void __launch_bounds__(256) k_scan_add(uint32_t* __restrict__ out, uint32_t n,
+                                                  const uint32_t* __restrict__ bsum) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += bsum[i / 4096u];
+}
+
+__global__ void __launch_bounds__(256) k_tile_fan(const uint32_t* __restrict__ off, uint32_t A, uint32_t T,
+                                                  uint32_t* __restrict__ fan, uint32_t* __restrict__ axn) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= T) return;
+  const uint32_t a0 = j * kTileN, a1 = min(a0 + kTileN, A);
+  fan[j] = off[a1] - off[a0];
+  axn[j] = a1 - a0;
+}
+
+__global__ void k_learn_index_done(LearnCtl* c, const ShardCtl* sc) {
+  c->row_sum = sc->row_sum;
+  c->ticks_seen = 0;
+  c->feat_done = 0;
+  c->prev_learned = 0;
+  c->eval_next = 0;
+  c->eval_now = 0;
+  for (int q = 0; q < 9; q++) c->inrate[q] = 0.f;
+}
+
+// ---------------------------------------------------------------------------
+// MLP training: forward + backward over a slice of the minibatch per block
+// (128 threads = the hidden units), partial gradients per block, a fixed-order
+// reduction, Adam.  Loss: mean squared error over the minibatch.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_mlp_grad(const __nv_bfloat16* __restrict__ wb, const float* __restrict__ X,
+                                                  const float* __restrict__ Yt, const uint32_t* __restrict__ idx,
+                                                  uint32_t count, uint32_t per, float inv_count,
+                                                  float* __restrict__ partial) {
+  __shared__ float xs[kFeat];
+  __shared__ float red[4];
+  __shared__ float s_dy;
+  const uint32_t u = threadIdx.x;
+  const float w2 = __bfloat162float(wb[kOffW2 + u]);
+  float g1[kFeat];
+#pragma unroll
+  for (int k = 0; k < (int)kFeat; k++) g1[k] = 0.f;
+  float gb1 = 0.f, gw2 = 0.f, gb2 = 0.f, loss = 0.f;
+  const uint32_t s0 = blockIdx.x * per, s1 = min(count, s0 + per);
+  for (uint32_t s = s0; s < s1; s++) {
+    const uint32_t id = idx ? idx[s] : s;
+    if (u < kFeat) xs[u] = bf16r(X[(size_t)id * kFeat + u]);
+    __syncthreads();
+    float a, hb;
+    const float y = mlp_block_forward(wb, xs, red, &a, &hb);
+    if (u == 0) {
+      const float d = __fsub_rn(y, Yt[id]);
+      s_dy = __fmul_rn(__fmul_rn(2.f, d), inv_count);
+      loss = fmaf(__fmul_rn(d, d), inv_count, loss);
+    }
+    __syncthreads();
+    const float dy = s_dy;
+    gw2 = fmaf(dy, hb, gw2);
+    if (u == 0) gb2 = __fadd_rn(gb2, dy);
+    const float dh = a > 0.f ? __fmul_rn(dy, w2) : 0.f;
+    gb1 = __fadd_rn(gb1, dh);
+#pragma unroll
+    for (int k = 0; k < (int)kFeat; k++) g1[k] = fmaf(dh, xs[k], g1[k]);
+    __syncthreads();
+  }
+  float* Pp = partial + (size_t)blockIdx.x * (kParams + 1);
+#pragma unroll
+  for (int k = 0; k < (int)kFeat; k++) Pp[u * kFeat + k] = g1[k];
+  Pp[kOffB1 + u] = gb1;
+  Pp[kOffW2 + u] = gw2;
+  if (u == 0) {
+    Pp[kOffB2] = gb2;
+    Pp[kParams] = loss;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mlp_reduce(const float* __restrict__ partial, uint32_t nb,
+                                                    float* __restrict__ grad) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > kParams) return;
+  float s = 0.f;
+  for (uint32_t b = 0; b < nb; b++) s = __fadd_rn(s, partial[(size_t)b * (kParams + 1) + p]);
+  grad[p] = s;
+}
+
+__global__ void __launch_bounds__(256) k_mlp_to_bf16(const float* __restrict__ master, __nv_bfloat16* __restrict__ wb) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < kParams) wb[p] = __float2bfloat16_rn(master[p]);
+}
+
+__global__ void __launch_bounds__(256) k_mlp_adam(float* __restrict__ master, float* __restrict__ m1,
+                                                  float* __restrict__ m2, const float* __restrict__ grad,
+                                                  __nv_bfloat16* __restrict__ wb, float lr, float c1, float c2,
+                                                  float* __restrict__ loss_acc) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p == 0) *loss_acc += grad[kParams];
+  if (p >= kParams) return;
+  const float g = grad[p];
+  const float a = 0.9f * m1[p] + 0.1f * g;
+  const float b = 0.999f * m2[p] + 0.001f * g * g;
+  m1[p] = a;
+  m2[p] = b;
+  const float w = master[p] - lr * (a * c1) / (sqrtf(b * c2) + 1e-8f);
+  master[p] = w;
+  wb[p] = __float2bfloat16_rn(w);
+}
+
+__global__ void __launch_bounds__(128) k_mlp_predict(const __nv_bfloat16* __restrict__ wb,
+                                                     const float* __restrict__ X, uint32_t count,
+                                                     float* __restrict__ out) {
+  __shared__ float xs[kFeat];
+  __shared__ float red[4];
+  for (uint32_t s = blockIdx.x; s < count; s += gridDim.x) {
+    if (threadIdx.x < kFeat) xs[threadIdx.x] = bf16r(X[(size_t)s * kFeat + threadIdx.x]);
+    __syncthreads();
+    const float y = mlp_block_forward(wb, xs, red, nullptr, nullptr);
+    if (threadIdx.x == 0) out[s] = y;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+}  // namespace axc
+
+// ===========================================================================
+// host side
+// ===========================================================================
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+namespace axc {
+namespace {
+
+__global__ void k_learn_set_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopamine) {
+  ctl->tick_base = tick_base;
+  ctl->dopamine = dopamine;
+}
+
+// splitmix64: seeded parameter init and minibatch order, identical on every host.
+inline uint64_t smix(uint64_t& x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+struct Learned {
+  ShardVramPtrs v{};
+  uint32_t N = 0, A = 0, voff = 0, nv = 0, words = 0, v_seg = 0, T = 0, tick_base = 0;
+  int16_t dopamine = 0;
+  const uint32_t* bits = nullptr;   // caller's device input bitmask [bits_ticks][words]
+  uint32_t bits_ticks = 0;
+  uint32_t sample_cap = 0;
+  void* base = nullptr;
+  LearnCtl* ctl = nullptr;
+  uint32_t *inv_off = nullptr, *fan = nullptr, *axn = nullptr, *yacc = nullptr, *bacc = nullptr, *fill = nullptr;
+  uint32_t *cap = nullptr, *seg = nullptr, *entries = nullptr, *alist = nullptr, *evbits = nullptr, *spk = nullptr;
+  uint32_t *deg = nullptr, *bsum = nullptr, *idx = nullptr;
+  int32_t* acc = nullptr;
+  float *hist = nullptr, *feat = nullptr, *pred = nullptr, *X = nullptr, *Y = nullptr;
+  float *master = nullptr, *m1 = nullptr, *m2 = nullptr, *grad = nullptr, *loss_acc = nullptr;
+  __nv_bfloat16* wb = nullptr;
+  uint32_t* inv = nullptr;
+  uint8_t* inv_seg = nullptr;
+  size_t inv_cap = 0;
+  uint32_t* stage = nullptr;
+  uint32_t stage_ticks = 0;
+  float* partial = nullptr;
+  uint32_t partial_blocks = 0;
+  uint32_t adam_step = 0;
+  int32_t policy = -1;
+  uint32_t collect = 0;
+  const void* rows_base = nullptr;   // the row cache the graphs were captured with
+  std::map<std::tuple<uint32_t, uint32_t>, cudaGraphExec_t> graphs;
+  cudaStream_t capture = nullptr;
+
+  LearnDev dev() const {
+    LearnDev d;
+    d.ctl = ctl;
+    d.inv_off = inv_off;
+    d.yacc = yacc;
+    d.bacc = bacc;
+    d.fill = fill;
+    d.cap = cap;
+    d.seg = seg;
+    d.alist = alist;
+    d.evbits = evbits;
+    return d;
+  }
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+};
+
+static void learned_free(Learned* L) {
+  if (!L) return;
+  L->drop_graphs();
+  if (L->capture) cudaStreamDestroy(L->capture);
+  void* ptrs[] = {L->base, L->inv, L->inv_seg, L->stage, L->partial};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete L;
+}
+
+static cudaError_t learned_partial(Learned& L, uint32_t blocks) {
+  if (L.partial_blocks >= blocks) return cudaSuccess;
+  if (L.partial) cudaFree(L.partial);
+  L.partial = nullptr;
+  L.partial_blocks = 0;
+  cudaError_t e = cudaMalloc(&L.partial, (size_t)blocks * (kParams + 1) * 4);
+  if (e == cudaSuccess) L.partial_blocks = blocks;
+  return e;
+}
+
+// The inverted index of the current targets (and the tile fan-outs), built
+// from the neuron-major rows; resets the feature history.
+static cudaError_t learned_index(Learned& L, cudaStream_t st) {
+  cudaError_t e;
+  ShardScratch* s = scratch_for(&L.v, L.N, L.A, &e);
+  if (!s) return e;
+  e = rows_alloc(*s, L.N, L.A);
+  if (e != cudaSuccess) return e;
+  e = launch_rows_begin(L.v, *s, L.N, L.A, st);
+  if (e != cudaSuccess) return e;
+  const RowCache& r = *s->rows;
+  e = cudaMemsetAsync(L.deg, 0, (size_t)L.A * 4, st);
+  if (e != cudaSuccess) return e;
+  const size_t slots = (size_t)L.N * kRowStride;
+  const uint32_t gb = (uint32_t)((slots + 255) / 256);
+  if (slots) k_inv_count<<<gb, 256, 0, st>>>(r.rt, r.cnt, L.N, L.A, L.deg);
+  const uint32_t nb = (L.A + 4095) / 4096;
+  if (nb > 4096) return cudaErrorInvalidValue;   // the two-level scan covers 16M axons
+  k_scan_blocks<<<std::max(nb, 1u), 1024, 0, st>>>(L.deg, L.inv_off, L.A, L.bsum);
+  k_scan_sums<<<1, 1024, 0, st>>>(L.bsum, std::max(nb, 1u), L.inv_off, L.A);
+  k_scan_add<<<(L.A + 255) / 256, 256, 0, st>>>(L.inv_off, L.A, L.bsum);
+  uint32_t total = 0;
+  e = cudaMemcpyAsync(&total, L.inv_off + L.A, 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  if (total > L.inv_cap || !L.inv) {
+    if (L.inv) cudaFree(L.inv);
+    if (L.inv_seg) cudaFree(L.inv_seg);
+    L.inv = nullptr;
+    L.inv_seg = nullptr;
+    L.inv_cap = 0;
+    const size_t want = std::max<size_t>(total, 1);
+    e = cudaMalloc(&L.inv, want * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&L.inv_seg, want);
+    if (e != cudaSuccess) return e;
+    L.inv_cap = want;
+    L.drop_graphs();
+  }
+  e = cudaMemcpyAsync(L.deg, L.inv_off, (size_t)L.A * 4, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  if (slots) k_inv_fill<<<gb, 256, 0, st>>>(r.rt, r.cnt, L.N, L.A, L.deg, L.inv, L.inv_seg);
+  k_tile_fan<<<(L.T + 255) / 256, 256, 0, st>>>(L.inv_off, L.A, L.T, L.fan, L.axn);
+  e = cudaMemsetAsync(L.hist, 0, (size_t)L.T * kHistF * 4, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(L.yacc, 0, (size_t)L.T * 4, st);
+  if (e != cudaSuccess) return e;
+  k_learn_index_done<<<1, 1, 0, st>>>(L.ctl, s->ctl);
+  return cudaGetLastError();
+}
+
+// One tick: schedule, prologue, both update forms (one of them returns at
+// once), fix-up, push, features + prediction.
+static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool features_on, cudaStream_t st) {
+  RowCache& r = *s.rows;
+  const uint32_t N = L.N, A = L.A;
+  const int sms = sm_count();
+  const LearnDev D = L.dev();
+  const uint32_t* bits_k = L.nv ? L.stage + (size_t)k * L.words : nullptr;
+  k_learn_plan<<<1, 1024, 0, st>>>(D, L.pred, L.fan, L.axn, L.cap, L.seg, L.entries, bits_k, L.words, L.nv, s.ctl,
+                                   features_on ? 1u : 0u);
+  const uint32_t G = std::max(A, N);
+  const uint32_t raise = (bits_k && ((uint64_t)L.voff + L.nv > A)) ? AXC_ERR_VIRTUAL_RANGE : 0u;
+  if (G)
+    k_rows_prologue<true><<<(G + 255) / 256, 256, 0, st>>>(L.v.axon_heads, A, L.v_seg, bits_k, L.voff,
+                                                           bits_k ? L.nv : 0u, s.incoming, nullptr, k, r.mask2,
+                                                           r.mult, L.v.soma_flags, L.v.timers, N, r.eval, s.ctl,
+                                                           raise, r.lit, D);
+  const uint32_t fix_cap = kFixCap;
+  const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
+  if (lit_bytes <= lit_smem_limit())
+    k_rows_update<true><<<sms, 1024, lit_bytes, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                     s.ctl, k, fix_cap, r.lit, L.ctl);
+  else
+    k_rows_update<false><<<4 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                   s.ctl, k, fix_cap, r.lit, L.ctl);
+  k_learn_scatter<<<4 * sms, 256, 0, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw, L.v.soma_flags, L.v.axon_heads,
+                                           A, L.acc, s.ctl);
+  k_learn_update<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, L.spk, s.ctl, k);
+  k_learn_gsop<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.rt, r.rw, r.cnt, r.mask2, L.spk, r.fix, s.ctl, fix_cap);
+  k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k);
+  k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
+                                       nullptr, nullptr, 0, s.ctl, k);
+  if (features_on && L.T)
+    k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.wb, L.X, L.Y,
+                                          L.nv ? L.stage + (size_t)(k + 1) * L.words : nullptr, L.words, L.nv);
+  return cudaGetLastError();
+}
+
+}  // namespace axc
+
+using namespace axc;
+
+extern "C" {
+
+uint32_t axc_mlp_param_count(void) { return kParams; }
+
+int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
+  if (!d || !out_handle || !d->vram.axon_heads || d->total_axons == 0) return (int32_t)cudaErrorInvalidValue;
+  if (d->d_input_bitmask && (d->words_per_tick == 0 || d->bitmask_ticks == 0)) return (int32_t)cudaErrorInvalidValue;
+  Learned* L = new Learned();
+  L->v = d->vram;
+  L->N = d->padded_n;
+  L->A = d->total_axons;
+  L->voff = d->virtual_offset;
+  L->nv = d->d_input_bitmask ? d->num_virtual : 0;
+  L->words = d->words_per_tick;
+  L->v_seg = d->v_seg;
+  L->dopamine = d->dopamine;
+  L->tick_base = d->tick_base;
+  L->bits = d->d_input_bitmask;
+  L->bits_ticks = d->d_input_bitmask ? d->bitmask_ticks : 0;
+  L->sample_cap = d->sample_capacity;
+  L->T = (L->A + kTileN - 1) / kTileN;
+  const uint32_t T = L->T, N = L->N, A = L->A;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t off = 0;
+  auto take = [&](size_t bytes) { const size_t o = off; off = al(off + bytes); return o; };
+  const size_t o_ctl = take(sizeof(LearnCtl));
+  const size_t o_off = take(((size_t)A + 1) * 4), o_fan = take((size_t)T * 4), o_axn = take((size_t)T * 4);
+  const size_t o_yacc = take((size_t)T * 4), o_bacc = take((size_t)T * 4), o_fill = take((size_t)T * 4);
+  const size_t o_cap = take((size_t)T * 4), o_seg = take(((size_t)T + 1) * 4), o_ent = take((size_t)T * 4);
+  const size_t o_alist = take((size_t)A * 4), o_ev = take(((size_t)N / 32 + 2) * 4), o_spk = take((size_t)N * 4 + 4);
+  const size_t o_deg = take((size_t)A * 4), o_bsum = take(4097 * 4), o_idx = take((size_t)L->sample_cap * 4 + 4);
+  const size_t o_acc = take((size_t)N * 4 + 4);
+  const size_t o_hist = take((size_t)T * kHistF * 4), o_feat = take((size_t)T * kFeat * 4);
+  const size_t o_pred = take((size_t)T * 4);
+  const size_t o_X = take((size_t)L->sample_cap * kFeat * 4), o_Y = take((size_t)L->sample_cap * 4);
+  const size_t o_master = take((size_t)kParams * 4), o_m1 = take((size_t)kParams * 4), o_m2 = take((size_t)kParams * 4);
+  const size_t o_grad = take(((size_t)kParams + 1) * 4), o_loss = take(4), o_wb = take((size_t)kParams * 2);
+  cudaError_t e = cudaMalloc(&L->base, off);
+  if (e == cudaSuccess) e = cudaMemset(L->base, 0, off);
+  if (e != cudaSuccess) {
+    learned_free(L);
+    return (int32_t)e;
+  }
+  char* b = static_cast<char*>(L->base);
+  L->ctl = reinterpret_cast<LearnCtl*>(b + o_ctl);
+  L->inv_off = reinterpret_cast<uint32_t*>(b + o_off);
+  L->fan = reinterpret_cast<uint32_t*>(b + o_fan);
+  L->axn = reinterpret_cast<uint32_t*>(b + o_axn);
+  L->yacc = reinterpret_cast<uint32_t*>(b + o_yacc);
+  L->bacc = reinterpret_cast<uint32_t*>(b + o_bacc);
+  L->fill = reinterpret_cast<uint32_t*>(b + o_fill);
+  L->cap = reinterpret_cast<uint32_t*>(b + o_cap);
+  L->seg = reinterpret_cast<uint32_t*>(b + o_seg);
+  L->entries = reinterpret_cast<uint32_t*>(b + o_ent);
+  L->alist = reinterpret_cast<uint32_t*>(b + o_alist);
+  L->evbits = reinterpret_cast<uint32_t*>(b + o_ev);
+  L->spk = reinterpret_cast<uint32_t*>(b + o_spk);
+  L->deg = reinterpret_cast<uint32_t*>(b + o_deg);
+  L->bsum = reinterpret_cast<uint32_t*>(b + o_bsum);
+  L->idx = reinterpret_cast<uint32_t*>(b + o_idx);
+  L->acc = reinterpret_cast<int32_t*>(b + o_acc);
+  L->hist = reinterpret_cast<float*>(b + o_hist);
+  L->feat = reinterpret_cast<float*>(b + o_feat);
+  L->pred = reinterpret_cast<float*>(b + o_pred);
+  L->X = reinterpret_cast<float*>(b + o_X);
+  L->Y = reinterpret_cast<float*>(b + o_Y);
+  L->master = reinterpret_cast<float*>(b + o_master);
+  L->m1 = reinterpret_cast<float*>(b + o_m1);
+  L->m2 = reinterpret_cast<float*>(b + o_m2);
+  L->grad = reinterpret_cast<float*>(b + o_grad);
+  L->loss_acc = reinterpret_cast<float*>(b + o_loss);
+  L->wb = reinterpret_cast<__nv_bfloat16*>(b + o_wb);
+  // control block defaults
+  LearnCtl hc;
+  std::memset(&hc, 0, sizeof(hc));
+  hc.sample_cap = L->sample_cap;
+  hc.sample_every = 1;
+  hc.policy = -1;
+  hc.ratio = 4.f;
+  hc.margin = 0.25f;
+  hc.slack = 64;
+  hc.T = T;
+  // seeded uniform init (fan-in scaled), biases 0
+  std::vector<float> w(kParams, 0.f);
+  uint64_t sd = 0xA11CE5EEDull;
+  for (uint32_t p = 0; p < kParams; p++) {
+    const float u = (float)(smix(sd) >> 40) * (1.f / 16777216.f) * 2.f - 1.f;
+    if (p < kOffB1) w[p] = u * 0.30618622f;              // sqrt(6 / 64)
+    else if (p >= kOffW2 && p < kOffB2) w[p] = u * 0.21650635f;   // sqrt(6 / 128)
+  }
+  e = cudaMemcpy(L->ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(L->master, w.data(), (size_t)kParams * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_mlp_to_bf16<<<(kParams + 255) / 256, 256>>>(L->master, L->wb);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->capture, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = learned_index(*L, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    learned_free(L);
+    return (int32_t)e;
+  }
+  *out_handle = L;
+  return 0;
+}
+
+void axc_learned_destroy(void* handle) { learned_free(static_cast<Learned*>(handle)); }
+
+int32_t axc_learned_refresh(void* handle, void* stream_v) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L) return (int32_t)cudaErrorInvalidValue;
+  return (int32_t)learned_index(*L, static_cast<cudaStream_t>(stream_v));
+}
+
+int32_t axc_learned_set_policy(void* handle, int32_t policy, float ratio, float margin, uint32_t slack) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L || policy < -1 || policy > 1 || !(ratio >= 0.f) || !(margin >= 0.f)) return (int32_t)cudaErrorInvalidValue;
+  cudaError_t e = cudaDeviceSynchronize();
+  LearnCtl hc;
+  if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return (int32_t)e;
+  hc.policy = policy;
+  hc.ratio = ratio;
+  hc.margin = margin;
+  hc.slack = slack;
+  L->policy = policy;
+  return (int32_t)cudaMemcpy(L->ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice);
+}
+
+int32_t axc_learned_collect(void* handle, uint32_t enable, uint32_t sample_every, uint32_t reset) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L || sample_every == 0) return (int32_t)cudaErrorInvalidValue;
+  cudaError_t e = cudaDeviceSynchronize();
+  LearnCtl hc;
+  if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return (int32_t)e;
+  hc.collect = enable ? 1u : 0u;
+  hc.sample_every = sample_every;
+  if (reset) hc.samples = 0;
+  L->collect = hc.collect;
+  return (int32_t)cudaMemcpy(L->ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice);
+}
+
+int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t tpg, void* stream_v) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L || tpg == 0 || ticks % tpg) return (int32_t)cudaErrorInvalidValue;
+  if (L->bits && (uint64_t)tick0 + ticks > L->bits_ticks) return (int32_t)cudaErrorInvalidValue;
+  cudaStream_t st = static_cast<cudaStream_t>(stream_v);
+  cudaError_t e;
+  ShardScratch* s = scratch_for(&L->v, L->N, L->A, &e);
+  if (!s) return (int32_t)e;
+  e = rows_alloc(*s, L->N, L->A);
+  if (e != cudaSuccess) return (int32_t)e;
+  if (L->rows_base != s->rows->base) {
+    L->drop_graphs();
+    L->rows_base = s->rows->base;
+  }
+  if (L->stage_ticks < tpg + 1) {
+    if (L->stage) cudaFree(L->stage);
+    L->stage = nullptr;
+    L->stage_ticks = 0;
+    e = cudaMalloc(&L->stage, (size_t)(tpg + 1) * std::max(L->words, 1u) * 4);
+    if (e != cudaSuccess) return (int32_t)e;
+    L->stage_ticks = tpg + 1;
+    L->drop_graphs();
+  }
+  const bool features_on = L->policy < 0 || L->collect;
+  const auto key = std::make_tuple(tpg, features_on ? 1u : 0u);
+  cudaGraphExec_t exec = nullptr;
+  auto it = L->graphs.find(key);
+  if (it != L->graphs.end()) {
+    exec = it->second;
+  } else {
+    e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return (int32_t)e;
+    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture);
+    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = learned_tick(*L, *s, k, features_on, L->capture);
+    if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(L->capture, &g);
+    if (le != cudaSuccess) e = le;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return (int32_t)e;
+    L->graphs[key] = exec;
+  }
+  for (uint32_t c = 0; c < ticks / tpg && e == cudaSuccess; c++) {
+    const uint32_t t0 = tick0 + c * tpg;
+    if (L->bits) {
+      const uint32_t have = std::min(tpg + 1, L->bits_ticks - t0);
+      e = cudaMemcpyAsync(L->stage, L->bits + (size_t)t0 * L->words, (size_t)have * L->words * 4,
+                          cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess && have < tpg + 1)
+        e = cudaMemsetAsync(L->stage + (size_t)have * L->words, 0, (size_t)(tpg + 1 - have) * L->words * 4, st);
+      if (e != cudaSuccess) break;
+    }
+    k_learn_set_ctl<<<1, 1, 0, st>>>(s->ctl, L->tick_base + t0, (int32_t)L->dopamine);
+    e = launch_reset_burst(L->v, L->N, st);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+  }
+  return (int32_t)e;
+}
+
+int32_t axc_learned_stats(void* handle, uint64_t* out16) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L || !out16) return (int32_t)cudaErrorInvalidValue;
+  cudaError_t e = cudaDeviceSynchronize();
+  LearnCtl hc;
+  if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return (int32_t)e;
+  for (int q = 0; q < 12; q++) out16[q] = hc.stat[q];
+  out16[12] = hc.samples;
+  out16[13] = hc.ticks_seen;
+  out16[14] = hc.T;
+  out16[15] = L->inv_cap;
+  return 0;
+}
+
+int32_t axc_learned_reset_stats(void* handle) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L) return (int32_t)cudaErrorInvalidValue;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess)
+    e = cudaMemset(reinterpret_cast<char*>(L->ctl) + offsetof(LearnCtl, stat), 0, sizeof(LearnCtl::stat));
+  return (int32_t)e;
+}
+
+int32_t axc_learned_params(void* handle, float* host_out, const float* host_in) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L) return (int32_t)cudaErrorInvalidValue;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && host_out) e = cudaMemcpy(host_out, L->master, (size_t)kParams * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && host_in) {
+    e = cudaMemcpy(L->master, host_in, (size_t)kParams * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(L->m1, 0, (size_t)kParams * 4);
+    if (e == cudaSuccess) e = cudaMemset(L->m2, 0, (size_t)kParams * 4);
+    if (e == cudaSuccess) {
+      k_mlp_to_bf16<<<(kParams + 255) / 256, 256>>>(L->master, L->wb);
+      e = cudaGetLastError();
+    }
+    L->adam_step = 0;
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return (int32_t)e;
+}
+
+// Adam on the recorded pairs: the first 90% (in recording order) train, the
+// last 10% validate.  out_loss[epoch] = mean training loss of the epoch.
+int32_t axc_learned_train(void* handle, uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float* out_loss,
+                          float* out_val, void* stream_v) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L || batch == 0 || !(lr > 0.f)) return (int32_t)cudaErrorInvalidValue;
+  cudaStream_t st = static_cast<cudaStream_t>(stream_v);
+  cudaError_t e = cudaDeviceSynchronize();
+  uint32_t n = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpy(&n, reinterpret_cast<char*>(L->ctl) + offsetof(LearnCtl, samples), 4, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return (int32_t)e;
+  const uint32_t nval = n / 10, ntr = n - nval;
+  if (ntr == 0) return (int32_t)cudaErrorInvalidValue;
+  const uint32_t maxb = std::max((std::min(batch, ntr) + kGradPer - 1) / kGradPer, (nval + kGradPer - 1) / kGradPer);
+  e = learned_partial(*L, std::max(maxb, 1u));
+  if (e != cudaSuccess) return (int32_t)e;
+  std::vector<uint32_t> order(ntr);
+  for (uint32_t i = 0; i < ntr; i++) order[i] = i;
+  uint64_t sd = seed;
+  for (uint32_t ep = 0; ep < epochs && e == cudaSuccess; ep++) {
+    for (uint32_t i = ntr - 1; i > 0; i--) std::swap(order[i], order[(uint32_t)(smix(sd) % (uint64_t)(i + 1))]);
+    e = cudaMemcpyAsync(L->idx, order.data(), (size_t)ntr * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(L->loss_acc, 0, 4, st);
+    uint32_t steps = 0;
+    for (uint32_t b0 = 0; b0 < ntr && e == cudaSuccess; b0 += batch) {
+      const uint32_t cnt = std::min(batch, ntr - b0);
+      const uint32_t nb = (cnt + kGradPer - 1) / kGradPer;
+      k_mlp_grad<<<nb, 128, 0, st>>>(L->wb, L->X, L->Y, L->idx + b0, cnt, kGradPer, 1.f / (float)cnt, L->partial);
+      k_mlp_reduce<<<(kParams + 1 + 255) / 256, 256, 0, st>>>(L->partial, nb, L->grad);
+      L->adam_step++;
+      const float c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)L->adam_step)));
+      const float c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)L->adam_step)));
+      k_mlp_adam<<<(kParams + 255) / 256, 256, 0, st>>>(L->master, L->m1, L->m2, L->grad, L->wb, lr, c1, c2,
+                                                       L->loss_acc);
+      e = cudaGetLastError();
+      steps++;
+    }
+    float tot = 0.f;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&tot, L->loss_acc, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (out_loss) out_loss[ep] = steps ? tot / (float)steps : 0.f;
+  }
+  if (e == cudaSuccess && out_val) {
+    *out_val = 0.f;
+    if (nval) {
+      const uint32_t nb = (nval + kGradPer - 1) / kGradPer;
+      k_mlp_grad<<<nb, 128, 0, st>>>(L->wb, L->X + (size_t)ntr * kFeat, L->Y + ntr, nullptr, nval, kGradPer,
+                                     1.f / (float)nval, L->partial);
+      k_mlp_reduce<<<(kParams + 1 + 255) / 256, 256, 0, st>>>(L->partial, nb, L->grad);
+      e = cudaMemcpyAsync(out_val, L->grad + kParams, 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+  }
+  return (int32_t)e;
+}
+
+// Copies recorded pairs out (rows [first, first + count)).
+int32_t axc_learned_samples(void* handle, uint32_t first, uint32_t count, float* host_x, float* host_y) {
+  Learned* L = static_cast<Learned*>(handle);
+  if (!L || (uint64_t)first + count > L->sample_cap) return (int32_t)cudaErrorInvalidValue;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && host_x)
+    e = cudaMemcpy(host_x, L->X + (size_t)first * kFeat, (size_t)count * kFeat * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && host_y) e = cudaMemcpy(host_y, L->Y + first, (size_t)count * 4, cudaMemcpyDeviceToHost);
+  return (int32_t)e;
+}
+
+// Stand-alone MLP entry points on caller buffers (FP32 parameters, rounded to
+// BF16 inside): the mean squared error and its gradient, and predictions.
+int32_t axc_mlp_loss_grad(const float* d_params, const float* d_x, const float* d_y, uint32_t count, float* d_grad,
+                          float* d_loss, void* stream_v) {
+  if (!d_params || !d_x || !d_y || !d_grad || count == 0) return (int32_t)cudaErrorInvalidValue;
+  cudaStream_t st = static_cast<cudaStream_t>(stream_v);
+  const uint32_t nb = (count + kGradPer - 1) / kGradPer;
+  __nv_bfloat16* wb = nullptr;
+  float *partial = nullptr, *grad = nullptr;
+  cudaError_t e = cudaMalloc(&wb, (size_t)kParams * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&partial, (size_t)nb * (kParams + 1) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&grad, ((size_t)kParams + 1) * 4);
+  if (e == cudaSuccess) {
+    k_mlp_to_bf16<<<(kParams + 255) / 256, 256, 0, st>>>(d_params, wb);
+    k_mlp_grad<<<nb, 128, 0, st>>>(wb, d_x, d_y, nullptr, count, kGradPer, 1.f / (float)count, partial);
+    k_mlp_reduce<<<(kParams + 1 + 255) / 256, 256, 0, st>>>(partial, nb, grad);
+    e = cudaMemcpyAsync(d_grad, grad, (size_t)kParams * 4, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && d_loss) e = cudaMemcpyAsync(d_loss, grad + kParams, 4, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  if (wb) cudaFree(wb);
+  if (partial) cudaFree(partial);
+  if (grad) cudaFree(grad);
+  return (int32_t)e;
+}
+
+int32_t axc_mlp_predict(const float* d_params, const float* d_x, uint32_t count, float* d_out, void* stream_v) {
+  if (!d_params || !d_x || !d_out) return (int32_t)cudaErrorInvalidValue;
+  if (count == 0) return 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream_v);
+  __nv_bfloat16* wb = nullptr;
+  cudaError_t e = cudaMalloc(&wb, (size_t)kParams * 2);
+  if (e == cudaSuccess) {
+    k_mlp_to_bf16<<<(kParams + 255) / 256, 256, 0, st>>>(d_params, wb);
+    k_mlp_predict<<<std::min(count, 4096u), 128, 0, st>>>(wb, d_x, count, d_out);
+    e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+  }
+  if (wb) cudaFree(wb);
+  return (int32_t)e;
+}
+
+}  // extern "C"

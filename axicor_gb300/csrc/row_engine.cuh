@@ -144,6 +144,58 @@ __device__ __forceinline__ bool fast_sensitive(uint32_t s, uint2 m) {
   return a0 != a1;
 }
 
+// Control block and per-tick buffers of the learned-schedule engine
+// (learned.cuh): the prologue accumulates per-tile activity into them and, on
+// a sparse tick, compacts the active axons into per-tile segments whose sizes
+// the predictor chose before the tick.
+struct LearnCtl {
+  uint32_t mode;          // this tick: 0 dense row pass, 1 sparse axon-driven gather
+  uint32_t overflow;      // a tile outgrew its pre-sized segment: the tick runs dense
+  uint32_t spk_count;     // sparse tick: spikers listed for GSOP
+  uint32_t stale;         // the inverted index no longer matches the targets
+  uint32_t ticks_seen;    // ticks completed with features since the history began
+  uint32_t samples;       // (features, target) pairs recorded
+  uint32_t sample_cap;
+  uint32_t sample_every;  // record every k-th tick
+  int32_t policy;         // -1 predictor, 0 always dense, 1 always sparse (exact capacities)
+  uint32_t collect;       // record pairs while running
+  float ratio;            // sparse when ratio * predicted active synapses < evaluated slots
+  float margin;           // capacity = prediction * (1 + margin) + slack
+  uint32_t slack;
+  uint32_t T;             // tiles of 1024 axons (= neurons)
+  uint32_t prev_mode;     // the previous tick's schedule
+  uint32_t prev_learned;  // the previous tick's schedule came from the predictor
+  uint32_t feat_done;     // the features kernel ran after the previous tick
+  uint32_t pad0;
+  unsigned long long eval_next;   // evaluated slots of the next tick (features kernel)
+  unsigned long long eval_now;    // evaluated slots of this tick
+  unsigned long long row_sum;     // targets checksum the inverted index was built from
+  float pred_total;               // sum of the tile predictions for this tick (synapses)
+  float inrate[9];                // input spike fraction of ticks t, t-1, ..., t-8
+  unsigned long long stat[12];
+};
+
+struct LearnDev {
+  LearnCtl* ctl;
+  const uint32_t* inv_off;  // [A+1] inverted index offsets (slots whose target is axon a)
+  uint32_t* yacc;           // [T] active synapses of the tile's axons this tick
+  uint32_t* bacc;           // [T] heads in flight on the tile's axons this tick
+  uint32_t* fill;           // [T] axons compacted into the tile's segment
+  const uint32_t* cap;      // [T] the tile's capacity in synapses
+  const uint32_t* seg;      // [T+1] segment offsets into alist
+  uint32_t* alist;          // active axons of a sparse tick
+  uint32_t* evbits;         // [N/32+1] evaluated neurons of the tick
+};
+
+// 64-bit mix of one live slot for the targets checksum (order-independent sum).
+__device__ __forceinline__ unsigned long long slot_mix(uint32_t t, uint32_t r) {
+  unsigned long long x = ((unsigned long long)t << 32) ^ (unsigned long long)r;
+  x *= 0x9E3779B97F4A7C15ull;
+  x ^= x >> 31;
+  x *= 0xBF58476D1CE4E5B9ull;
+  return x ^ (x >> 29);
+}
+
 // ---------------------------------------------------------------------------
 // batch start: columnar -> neuron-major, first-empty counts.
 // 32 neurons per 256-thread block; rows are read 8 at a time until every
@@ -182,6 +234,7 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     const uint32_t c = s_cnt[j];
     bool bad = false;
     uint32_t smx = 0;
+    unsigned long long hsum = 0;
     for (uint32_t q = lane; q < c; q += 32) {
       uint32_t t = s_t[q][j];
       // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
@@ -191,16 +244,19 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
         bad = true;
       }
       smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
+      hsum += slot_mix(t, n * kRowStride + q);
       rt[(size_t)n * kRowStride + q] = t;
       rw[(size_t)n * kRowStride + q] = s_w[q][j];
     }
     bad = __any_sync(kFull, bad);
     smx = __reduce_max_sync(kFull, smx);
+    hsum = warp_sum(hsum);
     if (lane == 0) {
       cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
       if (c) {
         atomicMax(&ctl->row_smax, c);
         atomicMax(&ctl->seg_max, smx);
+        atomicAdd(&ctl->row_sum, hsum + slot_mix(c, n));
       }
     }
   }
@@ -214,6 +270,7 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
     mask2[A] = make_uint2(0u, 0x80000000u);   // dummy entry of invalid targets: no hit, exact path
     ctl->row_smax = 0;
     ctl->seg_max = 0;
+    ctl->row_sum = 0;
   }
   if (n >= N) return;
   const uint32_t a = s2a[n];
@@ -242,11 +299,57 @@ __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ we
     if (r < c_mine) weights[(size_t)r * N + n0 + lane] = s_w[r][lane];
 }
 
+// Learned engine, in the prologue: per-tile active synapses and heads in
+// flight; on a sparse tick, the block's active axons go into its tile's
+// segment (a 256-thread block lies inside one 1024-axon tile).  A tile whose
+// actual activity exceeds its capacity sets the overflow flag.
+__device__ __forceinline__ void learn_axons(const LearnDev& L, uint32_t i, uint32_t A, uint32_t fan,
+                                            uint32_t inflight) {
+  __shared__ uint32_t s_red[3][8];
+  __shared__ uint32_t s_base2;
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool act = fan != 0u;
+  const uint32_t ball = __ballot_sync(kFull, act);
+  const uint32_t f = warp_sum(fan), b = warp_sum(inflight);
+  if (lane == 0) { s_red[0][w] = f; s_red[1][w] = b; s_red[2][w] = __popc(ball); }
+  __syncthreads();
+  const uint32_t i0 = blockIdx.x * blockDim.x;
+  const uint32_t j = i0 >> 10;
+  const bool sparse = L.ctl->mode == 1u;
+  if (threadIdx.x == 0) {
+    uint32_t tf = 0, tb = 0, tc = 0;
+    for (int q = 0; q < 8; q++) {
+      tf += s_red[0][q];
+      tb += s_red[1][q];
+      const uint32_t c = s_red[2][q];
+      s_red[2][q] = tc;
+      tc += c;
+    }
+    s_base2 = 0;
+    if (i0 < A) {
+      const uint32_t old = atomicAdd(&L.yacc[j], tf);
+      atomicAdd(&L.bacc[j], tb);
+      if (sparse && tc) {
+        s_base2 = atomicAdd(&L.fill[j], tc);
+        if (old + tf > L.cap[j] || s_base2 + tc > L.seg[j + 1] - L.seg[j]) L.ctl->overflow = 1u;
+      } else if (sparse && old + tf > L.cap[j]) {
+        L.ctl->overflow = 1u;
+      }
+    }
+  }
+  __syncthreads();
+  if (sparse && act) {
+    const uint32_t pos = s_base2 + s_red[2][w] + __popc(ball & ((1u << lane) - 1u));
+    if (pos < L.seg[j + 1] - L.seg[j]) L.alist[L.seg[j] + pos] = i;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // per tick 1/4: axons (inject, network pushes, propagate, split masks) and
 // somas (refractory countdown, list of neurons to evaluate).  The list entry
 // positions are reserved once per block.
 // ---------------------------------------------------------------------------
+template <bool LEARN>
 __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__ heads, uint32_t A, uint32_t v_seg,
                                                        const uint32_t* __restrict__ bitmask, uint32_t voff,
                                                        uint32_t nv, uint32_t* __restrict__ incoming,
@@ -255,7 +358,7 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint8_t* __restrict__ flags, uint8_t* __restrict__ timers,
                                                        uint32_t N, uint32_t* __restrict__ eval,
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err,
-                                                       uint32_t* __restrict__ lit_bits) {
+                                                       uint32_t* __restrict__ lit_bits, LearnDev L) {
   __shared__ uint32_t s_pmax, s_base, s_need;
   __shared__ int s_inc;
   __shared__ uint32_t s_warp[8];
@@ -272,6 +375,7 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
   __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool lit = false;
+  uint32_t fan = 0, inflight = 0;   // LEARN: active synapses and heads in flight of axon i
   if (i < A) {
     uint4* p = reinterpret_cast<uint4*>(heads + i);
     const uint4 x = p[0], y = p[1];
@@ -297,7 +401,13 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
     // most one soma owns the axon, so for those segments the hit is 1 and one
     // push cannot change it
     lit = (m.x & s_need) == s_need && !(m.y >> 31);
+    if (LEARN) {
+      if ((m.x | (m.y & 0x7FFFFFFFu)) != 0u) fan = __ldg(L.inv_off + i + 1) - __ldg(L.inv_off + i);
+#pragma unroll
+      for (int j = 0; j < 8; j++) inflight += h[j] < 255u + s_pmax ? 1u : 0u;
+    }
   }
+  if (LEARN) learn_axons(L, i, A, fan, inflight);
   if (lit_bits) {
     const uint32_t lb = __ballot_sync(kFull, lit);
     if ((threadIdx.x & 31) == 0 && i < A) lit_bits[i >> 5] = lb;
@@ -314,6 +424,7 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
   }
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t ballot = __ballot_sync(kFull, ev);
+  if (LEARN && lane == 0 && i < N) L.evbits[i >> 5] = ballot;
   if (lane == 0) s_warp[w] = __popc(ballot);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -365,6 +476,156 @@ __device__ __noinline__ int gsop_general(const BurstHeads8* heads, const uint2* 
   return 0;
 }
 
+// GSOP deltas per variant and inertia rank for a spiker (flags type | 0b101:
+// burst multiplier 2, physics.cu:255, 271-273, 290-291; physics.cu:336-349).
+// Called by the first 256 threads of the block.
+__device__ __forceinline__ void build_gtab(int2 (*gtab)[16], const VariantParameters* lut, int32_t dopamine) {
+  if (threadIdx.x < 256) {
+    const uint32_t v = threadIdx.x >> 4, r = threadIdx.x & 15;
+    const GsopConsts g = gsop_consts((uint8_t)((v << 4) | 0x05), lut[v], dopamine);
+    const int32_t inertia = lut[v].inertia_curve[r];
+    gtab[v][r] = make_int2(wmul(wmul(g.raw_pot, inertia), g.bm) >> 7, wmul(wmul(g.final_dep, inertia), g.bm) >> 7);
+  }
+}
+
+// The dendrite pass over the 16 slots one lane holds (slots 32j + 4g8 + i of
+// a row with c used slots): returns the lane's share of the input current and
+// sets, per slot (bit 4j+i), hitb = the segment is hit and slowb = GSOP needs
+// the exact path (physics.cu:186-207 for the hit test).
+template <bool LIT>
+__device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&W)[4], uint32_t c, uint32_t g8,
+                                             const uint2* __restrict__ mask2, const uint32_t* s_lit, uint32_t seg_hi,
+                                             bool exact, bool gfast, uint32_t prop, const BurstHeads8* heads,
+                                             uint32_t A, uint32_t& hitb_out, uint32_t& slowb_out) {
+  int32_t i_in = 0;
+  uint32_t hitb = 0, slowb = 0;   // bit 4j+i
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t q0 = 32u * j + 4u * g8;
+    uint2 m[4];
+    bool lit[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const uint32_t t = word_of(T[j], i);
+      const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
+      lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
+      m[i] = (q0 + i < c && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if (q0 + i >= c) continue;
+      if (LIT && lit[i]) {                      // segment 1..30 of a fully lit axon: hit, fast GSOP
+        i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+        hitb |= 1u << (4 * j + i);
+        continue;
+      }
+      const uint32_t t = word_of(T[j], i);
+      const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+      const uint32_t sh = min(s, 31u);
+      const uint32_t bx = (m[i].x >> sh) & 1u, by = (m[i].y >> sh) & 1u;
+      bool hit = (bx | by) != 0u;              // bit 31 (s >= 31): "may hit", tested below
+      if (hit && (s >= 31u || !exact))
+        hit = hit_exact(heads, A, (t & AXC_TARGET_AXON_MASK) - 1u, s, prop);
+      if (hit) {
+        i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+        hitb |= 1u << (4 * j + i);
+      }
+      // fast GSOP: hit decides, and one same-tick push could not change it
+      const bool fast = gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u));
+      slowb |= fast ? 0u : (1u << (4 * j + i));
+    }
+  }
+  hitb_out = hitb;
+  slowb_out = slowb;
+  return i_in;
+}
+
+// GLIF of one evaluated (non-refractory) neuron, physics.cu:209-275.
+struct GlifOut {
+  int32_t v, thr;
+  int glif, spike;
+};
+
+__device__ __forceinline__ GlifOut glif_step(const VariantParameters& p, int32_t v0, int32_t thr0, int32_t i_in,
+                                             uint32_t tick, uint32_t n) {
+  GlifOut o;
+  const int32_t decayed = wsub(thr0, (int32_t)p.homeostasis_decay);
+  int32_t thr = decayed & ~(decayed >> 31);
+  int32_t leak = p.leak_rate;
+  if (p.adaptive_mode == 1) {
+    leak = wadd(leak, wmul(thr, (int32_t)p.adaptive_leak_gain) >> 8);
+    const int32_t over = wsub(leak, p.adaptive_leak_max);
+    leak = wsub(leak, over & ~(over >> 31));
+  }
+  int32_t v = wadd(v0, i_in);
+  const int32_t diff = wsub(v, p.rest_potential);
+  const int32_t sign = (diff > 0) - (diff < 0);
+  int32_t leaked = wsub(wmul(diff, sign), leak);
+  leaked = leaked & ~(leaked >> 31);
+  v = wadd(p.rest_potential, wmul(sign, leaked));
+  const int glif = v >= wadd(p.threshold, thr) ? 1 : 0;
+  const uint32_t period = p.spontaneous_firing_period_ticks;
+  const int hb = (period > 0 && ((tick + n * 104729u) % period) == 0) ? 1 : 0;
+  if (glif) {
+    v = p.rest_potential;
+    thr = wadd(thr, p.homeostasis_penalty);
+  }
+  o.v = v;
+  o.thr = thr;
+  o.glif = glif;
+  o.spike = glif | hb;
+  return o;
+}
+
+// GSOP of a spiker's slots held by this lane (physics.cu:281-373): fast slots
+// from the gtab deltas, slow ones on the exact path or deferred to the fix-up
+// list.  Writes the changed weights back to the row; returns the slots done.
+__device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint32_t slowb, uint32_t c, uint32_t g8,
+                                             const int2 (*gtab)[16], uint32_t var, const uint32_t* trow,
+                                             int16_t* wrow, const BurstHeads8* heads, const uint2* mask2,
+                                             uint32_t A, const VariantParameters& p, uint8_t flags,
+                                             int32_t dopamine, ShardCtl* ctl, uint32_t* fix, uint32_t fix_cap,
+                                             uint32_t n) {
+  uint32_t gdone = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t q0 = 32u * j + 4u * g8;
+    if (q0 >= c) continue;
+    uint2 wj = W[j];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const uint32_t b = 1u << (4 * j + i);
+      if (q0 + i >= c) continue;
+      const int16_t w16 = half_of(wj, i);
+      if (!(slowb & b)) {
+        // cooling shift 0: delta = +potentiation or -depression of the weight's rank
+        const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+        const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
+        int32_t na = aw + ((hitb & b) ? e.x : -e.y);
+        na = min(max(na, 0), 32767);
+        set_half(wj, i, (int16_t)(w16 < 0 ? -na : na));
+        gdone++;
+        continue;
+      }
+      const uint32_t t = __ldg(trow + 32 * j + i);
+      int16_t nw = w16;
+      const int r = gsop_general(heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u, t >> AXC_TARGET_SEG_SHIFT, p,
+                                 flags, dopamine, &nw);
+      if (r == 2) continue;
+      gdone++;
+      if (r == 1) {
+        const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+        if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
+        else ctl->fix_overflow = 1u;
+        continue;
+      }
+      set_half(wj, i, nw);
+    }
+    if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
+  }
+  return gdone;
+}
+
 // LIT: 1024-thread blocks (one per SM) that first copy the prologue's
 // fully-lit bitmap (one bit per axon) into shared memory; slots whose axon is
 // fully lit need no mask gather from L2.
@@ -373,11 +634,13 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
     k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A, const uint32_t* __restrict__ rt,
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
                   const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
-                  ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits) {
+                  ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits,
+                  const LearnCtl* __restrict__ lc) {
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];   // GSOP (potentiation, depression) per variant and inertia rank
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
+  if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
   lut_to_smem(lut);
   if (threadIdx.x == 0) s_pmax = lut_pmax();
   if (LIT) {
@@ -387,14 +650,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   __syncthreads();
   const uint32_t tick = ctl->tick_base + k;
   const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
-  if (threadIdx.x < 256) {
-    // a spiker's flags after the update are type | 0b101, so its burst multiplier
-    // is 2 (physics.cu:255, 271-273, 290-291); physics.cu:336-349 for each rank
-    const uint32_t v = threadIdx.x >> 4, r = threadIdx.x & 15;
-    const GsopConsts g = gsop_consts((uint8_t)((v << 4) | 0x05), lut[v], dopamine);
-    const int32_t inertia = lut[v].inertia_curve[r];
-    gtab[v][r] = make_int2(wmul(wmul(g.raw_pot, inertia), g.bm) >> 7, wmul(wmul(g.final_dep, inertia), g.bm) >> 7);
-  }
+  build_gtab(gtab, lut, dopamine);
   __syncthreads();
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t smax = ctl->row_smax;   // longest row of the shard: rows are loaded up to here
@@ -437,44 +693,9 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       const bool exact = prop == s_pmax;
       const bool gfast = exact && prop <= 16u;
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
-      int32_t i_in = 0;
-      uint32_t hitb = 0, slowb = 0;   // bit 4j+i
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const uint32_t q0 = 32u * j + 4u * g8;
-        uint2 m[4];
-        bool lit[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const uint32_t t = word_of(T[j], i);
-          const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
-          lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
-          m[i] = (q0 + i < c && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
-        }
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          if (q0 + i >= c) continue;
-          if (LIT && lit[i]) {                      // segment 1..30 of a fully lit axon: hit, fast GSOP
-            i_in = wadd(i_in, (int32_t)half_of(W[j], i));
-            hitb |= 1u << (4 * j + i);
-            continue;
-          }
-          const uint32_t t = word_of(T[j], i);
-          const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
-          const uint32_t sh = min(s, 31u);
-          const uint32_t bx = (m[i].x >> sh) & 1u, by = (m[i].y >> sh) & 1u;
-          bool hit = (bx | by) != 0u;              // bit 31 (s >= 31): "may hit", tested below
-          if (hit && (s >= 31u || !exact))
-            hit = hit_exact(P.axon_heads, A, (t & AXC_TARGET_AXON_MASK) - 1u, s, prop);
-          if (hit) {
-            i_in = wadd(i_in, (int32_t)half_of(W[j], i));
-            hitb |= 1u << (4 * j + i);
-          }
-          // fast GSOP: hit decides, and one same-tick push could not change it
-          const bool fast = gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u));
-          slowb |= fast ? 0u : (1u << (4 * j + i));
-        }
-      }
+      uint32_t hitb, slowb;
+      int32_t i_in = row_slots<LIT>(T, W, c, g8, mask2, s_lit, seg_hi, exact, gfast, prop, P.axon_heads, A, hitb,
+                                    slowb);
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
@@ -483,33 +704,13 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       // GLIF (physics.cu:209-275); the neuron is not refractory
       int spike = 0;
       if (valid) {
-        const int32_t decayed = wsub(thr0, (int32_t)p.homeostasis_decay);
-        int32_t thr = decayed & ~(decayed >> 31);
-        int32_t leak = p.leak_rate;
-        if (p.adaptive_mode == 1) {
-          leak = wadd(leak, wmul(thr, (int32_t)p.adaptive_leak_gain) >> 8);
-          const int32_t over = wsub(leak, p.adaptive_leak_max);
-          leak = wsub(leak, over & ~(over >> 31));
-        }
-        int32_t v = wadd(v0, i_in);
-        const int32_t diff = wsub(v, p.rest_potential);
-        const int32_t sign = (diff > 0) - (diff < 0);
-        int32_t leaked = wsub(wmul(diff, sign), leak);
-        leaked = leaked & ~(leaked >> 31);
-        v = wadd(p.rest_potential, wmul(sign, leaked));
-        const int glif = v >= wadd(p.threshold, thr) ? 1 : 0;
-        const uint32_t period = p.spontaneous_firing_period_ticks;
-        const int hb = (period > 0 && ((tick + n * 104729u) % period) == 0) ? 1 : 0;
-        spike = glif | hb;
-        if (glif) {
-          v = p.rest_potential;
-          thr = wadd(thr, p.homeostasis_penalty);
-        }
+        const GlifOut o = glif_step(p, v0, thr0, i_in, tick, n);
+        spike = o.spike;
         if (g8 == 0) {
-          P.soma_voltage[n] = v;
+          P.soma_voltage[n] = o.v;
           P.soma_flags[n] = (uint8_t)((flags & 0xF0) | (spike ? 0x05 : 0x00));
-          P.threshold_offset[n] = thr;
-          P.timers[n] = glif ? p.refractory_period : 0;
+          P.threshold_offset[n] = o.thr;
+          P.timers[n] = o.glif ? p.refractory_period : 0;
           if (spike) {
             nspk++;
             const uint32_t my_axon = P.soma_to_axon[n];
@@ -521,44 +722,9 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
         }
       }
       // GSOP on the row in registers (physics.cu:281-373)
-      if (spike) {
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const uint32_t q0 = 32u * j + 4u * g8;
-          if (q0 >= c) continue;
-          uint2 wj = W[j];
-#pragma unroll
-          for (int i = 0; i < 4; i++) {
-            const uint32_t b = 1u << (4 * j + i);
-            if (q0 + i >= c) continue;
-            const int16_t w16 = half_of(wj, i);
-            if (!(slowb & b)) {
-              // cooling shift 0: delta = +potentiation or -depression of the weight's rank
-              const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
-              const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
-              int32_t na = aw + ((hitb & b) ? e.x : -e.y);
-              na = min(max(na, 0), 32767);
-              set_half(wj, i, (int16_t)(w16 < 0 ? -na : na));
-              gdone++;
-              continue;
-            }
-            const uint32_t t = __ldg(trow + 32 * j + i);
-            int16_t nw = w16;
-            const int r = gsop_general(P.axon_heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u,
-                                       t >> AXC_TARGET_SEG_SHIFT, p, flags, dopamine, &nw);
-            if (r == 2) continue;
-            gdone++;
-            if (r == 1) {
-              const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
-              if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q0 + i);
-              else ctl->fix_overflow = 1u;
-              continue;
-            }
-            set_half(wj, i, nw);
-          }
-          if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
-        }
-      }
+      if (spike)
+        gdone += row_gsop(W, hitb, slowb, c, g8, gtab, var, trow, wrow, P.axon_heads, mask2, A, p, flags, dopamine,
+                          ctl, fix, fix_cap, n);
     }
   }
   const uint32_t err_any = __reduce_or_sync(kFull, err);
@@ -770,18 +936,18 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   if (bitmask && ((uint64_t)a.virtual_offset + a.num_virtual > A)) raise |= AXC_ERR_VIRTUAL_RANGE;
   const uint32_t G = max(A, N);
   if (G)
-    k_rows_prologue<<<(G + 255) / 256, 256, 0, stream>>>(
+    k_rows_prologue<false><<<(G + 255) / 256, 256, 0, stream>>>(
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
-        raise, r.lit);
+        raise, r.lit, LearnDev{});
   if (ev) cudaEventRecord(ev[2], stream);
   const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
   if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                        s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit);
+                                                        s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit, nullptr);
   } else {
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                      s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit);
+                                                      s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit, nullptr);
   }
   if (ev) cudaEventRecord(ev[3], stream);
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k);

@@ -104,6 +104,28 @@ def config4(seed: int = 0xA11C4, ticks: int = 5000) -> Workload:
     return Workload("plain-8M", (200, 200, 200), 128, 8192, ticks, seed, default_lut(), rates)
 
 
+def sinusoid_rates(lo: float = 0.01, hi: float = 0.2, period: int = 100) -> np.ndarray:
+    """Per-tick input probability lo..hi..lo over `period` ticks (Q0.32)."""
+    return np.array([p_q32(lo + (hi - lo) * 0.5 * (1.0 - math.cos(2.0 * math.pi * t / period)))
+                     for t in range(period)], dtype=np.uint32)
+
+
+def homeostatic(w: Workload, penalty: int = 16000, decay: int = 80) -> Workload:
+    """The same brain with homeostasis on (each spike raises the neuron's
+    threshold offset by `penalty`, which then decays by `decay` per tick) and
+    the sinusoidal 0.01..0.2 input rate.  After a transient of about 300 ticks
+    a few neurons per thousand fire per tick and about 3% of the evaluated
+    slots are hit, following the 100-tick input cycle: the quiet regime the
+    learned schedule's sparse form is for."""
+    lut = w.lut.copy()
+    for v in (0, 1):
+        lut[v]["homeostasis_penalty"] = penalty
+        lut[v]["homeostasis_decay"] = decay
+    return Workload(w.name.replace("plain", "homeostatic"), w.dims, w.slots, w.num_inputs, w.ticks, w.seed, lut,
+                    sinusoid_rates(), w.v_seg, w.dopamine, w.inhibitory_permille, w.radius, w.lambda_voxels,
+                    w.w_min, w.w_max, dict(w.extra))
+
+
 def small(dims=(16, 16, 8), slots=64, inputs=64, p=0.08, ticks=50, seed=7, **lut_kw) -> Workload:
     """Small brains for parity tests."""
     return Workload(f"small-{dims[0]}x{dims[1]}x{dims[2]}", tuple(dims), slots, inputs, ticks, seed,

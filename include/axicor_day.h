@@ -367,6 +367,67 @@ void axc_population_destroy(void* handle);
  * axc_row_engine_fix_capacity, for tests of the rescan path). */
 uint32_t axc_population_fix_capacity(uint32_t cap);
 
+/* ---- Learned-schedule engine ------------------------------------------- */
+/* One brain stepped by the row engine, with a per-tile activity predictor (an
+ * MLP 64 -> 128 -> 1, BF16 weights, FP32 accumulation; tiles of 1024 axons)
+ * choosing before every tick between the dense row pass and a sparse,
+ * axon-driven gather through an inverted index, and sizing the per-tile
+ * compaction buffers of the sparse form.  A tile that outgrows its buffer
+ * makes the tick run dense, so every schedule gives the state of
+ * axc_step_day_phase_batch bit for bit.  The LUT is the process LUT
+ * (cu_upload_constant_memory).  No counterpart in the reference. */
+typedef struct AxcLearnedDesc {
+  ShardVramPtrs vram;                 /* from cu_allocate_shard, state uploaded */
+  uint32_t padded_n, total_axons;
+  uint32_t virtual_offset, num_virtual;
+  const uint32_t* d_input_bitmask;    /* device [bitmask_ticks][words_per_tick], or NULL */
+  uint32_t words_per_tick, bitmask_ticks;
+  uint32_t v_seg;
+  int32_t dopamine;
+  uint32_t tick_base;                 /* global tick of bitmask row 0 */
+  uint32_t sample_capacity;           /* (features, target) pairs kept for training */
+} AxcLearnedDesc;
+
+/* Builds the inverted index of the shard's current targets (synchronous). */
+int32_t axc_learned_create(const AxcLearnedDesc* desc, void** out_handle);
+/* Rebuilds the index after the targets changed (sort_and_prune, uploads).
+ * Until then ticks whose targets checksum differs run dense (stat [8]). */
+int32_t axc_learned_refresh(void* handle, void* stream);
+/* policy -1: the predictor picks; 0: always dense; 1: always sparse with
+ * exact (full fan-out) buffers.  Sparse is picked when
+ * ratio * predicted active synapses < next tick's evaluated slots; a tile's
+ * buffer holds prediction * (1 + margin) + slack synapses. */
+int32_t axc_learned_set_policy(void* handle, int32_t policy, float ratio, float margin, uint32_t slack);
+/* Records (features of tick t-1, active-synapse fraction of tick t) for every
+ * tile on every sample_every-th tick while enabled; reset drops the pairs. */
+int32_t axc_learned_collect(void* handle, uint32_t enable, uint32_t sample_every, uint32_t reset);
+/* Runs ticks [tick0, tick0 + ticks) (bitmask rows), graphs of ticks_per_graph
+ * ticks (ticks must be a multiple); asynchronous on `stream`. */
+int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t ticks_per_graph, void* stream);
+/* Adam over the recorded pairs (first 90% train, last 10% validate):
+ * out_loss[epochs] mean training MSE per epoch, *out_val validation MSE. */
+int32_t axc_learned_train(void* handle, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                          float* out_loss, float* out_val, void* stream);
+/* Host copies of the FP32 master parameters (W1[128][64], b1[128], w2[128],
+ * b2); either pointer may be NULL.  Setting them resets the Adam moments. */
+int32_t axc_learned_params(void* handle, float* host_out, const float* host_in);
+int32_t axc_learned_samples(void* handle, uint32_t first, uint32_t count, float* host_x, float* host_y);
+/* [0] ticks, [1] sparse ticks, [2] overflow re-runs, [3] schedule mismatches
+ * against exact counts, [4] sum |predicted - actual| active synapses over
+ * tiles, [5] sum actual, [6] judged ticks, [7] planned sparse, [8] stale-index
+ * ticks, [12] recorded pairs, [13] feature history length, [14] tiles,
+ * [15] index capacity. */
+int32_t axc_learned_stats(void* handle, uint64_t out[16]);
+int32_t axc_learned_reset_stats(void* handle);
+void axc_learned_destroy(void* handle);
+uint32_t axc_mlp_param_count(void);
+/* Mean squared error of the MLP (parameters FP32, rounded to BF16) over
+ * count samples x[count][64], y[count], and its gradient d_grad[param_count]
+ * (device buffers; synchronous). */
+int32_t axc_mlp_loss_grad(const float* d_params, const float* d_x, const float* d_y, uint32_t count,
+                          float* d_grad, float* d_loss, void* stream);
+int32_t axc_mlp_predict(const float* d_params, const float* d_x, uint32_t count, float* d_out, void* stream);
+
 /* ---- Synthetic brain generator (host) ---------------------------------- */
 /* Neurons fill a dim_x*dim_y*dim_z voxel grid (x fastest, one per voxel);
  * neuron n owns axon n; input v owns virtual axon padded_n + v and sits on a
