@@ -229,8 +229,8 @@ __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __
 }
 
 // ---------------------------------------------------------------------------
-// per tick 2s: the sparse gather.  A warp per active axon walks its slots in
-// the inverted index; hit slots of evaluated neurons add their weight to the
+// per tick 2s: the sparse gather.  The tiles' active axons, as one flat range,
+// a warp per axon walking the axon's slots in the inverted index; hit slots of evaluated neurons add their weight to the
 // neuron's input current (wrapping int32, order-independent).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, const uint32_t* __restrict__ inv,
@@ -245,36 +245,63 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
   if (c.mode != 1u || c.overflow) return;
   __shared__ uint32_t s_prop[16];
   __shared__ uint32_t s_pmax;
+  extern __shared__ uint32_t s_pre[];   // [T+1] prefix of the tiles' active-axon counts
   if (threadIdx.x < 16) s_prop[threadIdx.x] = VARIANT_LUT[threadIdx.x].signal_propagation_length;
   if (threadIdx.x == 0) s_pmax = lut_pmax();
-  __syncthreads();
+  // every block scans the fills itself: the tiles' active axons form one flat
+  // range [0, total) that all warps of the grid share
+  {
+    const uint32_t per = (T + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t t = 0;
+    for (uint32_t q = 0; q < per; q++)
+      if (b0 + q < T) t += min(L.fill[b0 + q], __ldg(L.seg + b0 + q + 1) - __ldg(L.seg + b0 + q));
+    __shared__ uint32_t s_part[256];
+    s_part[threadIdx.x] = t;
+    __syncthreads();
+    for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
+      const uint32_t x = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0u;
+      __syncthreads();
+      s_part[threadIdx.x] += x;
+      __syncthreads();
+    }
+    uint32_t run = s_part[threadIdx.x] - t;
+    for (uint32_t q = 0; q < per; q++)
+      if (b0 + q < T) {
+        s_pre[b0 + q] = run;
+        run += min(L.fill[b0 + q], __ldg(L.seg + b0 + q + 1) - __ldg(L.seg + b0 + q));
+      }
+    if (threadIdx.x == blockDim.x - 1) s_pre[T] = s_part[blockDim.x - 1];
+    __syncthreads();
+  }
+  const uint32_t total = s_pre[T];
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t total = L.seg[T];
   unsigned long long hits = 0;
   for (uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < total; e += nwarps) {
-    // the tile whose segment holds position e
-    uint32_t lo = 0, hi = T;
+    uint32_t lo = 0, hi = T;   // the tile holding flat position e
     while (hi - lo > 1) {
       const uint32_t mid = (lo + hi) >> 1;
-      if (__ldg(L.seg + mid) <= e) lo = mid; else hi = mid;
+      if (s_pre[mid] <= e) lo = mid; else hi = mid;
     }
-    if (e - __ldg(L.seg + lo) >= L.fill[lo]) continue;
-    const uint32_t a = L.alist[e];
+    const uint32_t a = L.alist[__ldg(L.seg + lo) + (e - s_pre[lo])];
     const uint2 m = __ldg(mask2 + a);
     const uint32_t r0 = __ldg(L.inv_off + a), r1 = __ldg(L.inv_off + a + 1);
     for (uint32_t r = r0 + lane; r < r1; r += 32) {
       const uint32_t s = inv_seg[r];
+      const uint32_t slot = __ldg(inv + r);
       const uint32_t sh = min(s, 31u);
       if (!(((m.x | m.y) >> sh) & 1u)) continue;
-      const uint32_t slot = __ldg(inv + r);
       const uint32_t n = slot / kRowStride;
-      if (!((__ldg(L.evbits + (n >> 5)) >> (n & 31u)) & 1u)) continue;
-      const uint32_t prop = s_prop[flags[n] >> 4];
+      const uint32_t evw = __ldg(L.evbits + (n >> 5));
+      const uint32_t fl = flags[n];
+      const int32_t wv = rw[slot];
+      if (!((evw >> (n & 31u)) & 1u)) continue;
+      const uint32_t prop = s_prop[fl >> 4];
       bool hit = true;
       if (s >= 31u || prop != s_pmax) hit = hit_exact(heads, A, a, s, prop);
       if (hit) {
-        atomicAdd(acc + n, (int32_t)rw[slot]);
+        atomicAdd(acc + n, wv);
         hits++;
       }
     }
@@ -869,7 +896,7 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool fe
   else
     k_rows_update<false><<<4 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                    s.ctl, k, fix_cap, r.lit, L.ctl);
-  k_learn_scatter<<<4 * sms, 256, 0, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw, L.v.soma_flags, L.v.axon_heads,
+  k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw, L.v.soma_flags, L.v.axon_heads,
                                            A, L.acc, s.ctl);
   k_learn_update<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, L.spk, s.ctl, k);
   k_learn_gsop<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.rt, r.rw, r.cnt, r.mask2, L.spk, r.fix, s.ctl, fix_cap);
@@ -964,7 +991,7 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   hc.sample_cap = L->sample_cap;
   hc.sample_every = 1;
   hc.policy = -1;
-  hc.ratio = 4.f;
+  hc.ratio = 3.f;
   hc.margin = 0.25f;
   hc.slack = 64;
   hc.T = T;
@@ -983,6 +1010,8 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->capture, cudaStreamNonBlocking);
+  if (e == cudaSuccess && ((size_t)T + 1) * 4 > 48 * 1024)
+    e = cudaFuncSetAttribute(k_learn_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(((size_t)T + 1) * 4));
   if (e == cudaSuccess) e = learned_index(*L, nullptr);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {

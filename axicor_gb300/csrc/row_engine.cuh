@@ -359,13 +359,15 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint32_t N, uint32_t* __restrict__ eval,
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err,
                                                        uint32_t* __restrict__ lit_bits, LearnDev L) {
-  __shared__ uint32_t s_pmax, s_base, s_need;
+  __shared__ uint32_t s_pmax, s_base, s_need, s_act;
   __shared__ int s_inc;
   __shared__ uint32_t s_warp[8];
   if (threadIdx.x == 0) {
     s_pmax = lut_pmax();
     const uint32_t hi = min(ctl->seg_max, 30u);   // segments 1..hi are the ones the batch's slots use
     s_need = hi ? (((2u << hi) - 1u) & ~1u) : 0xFFFFFFFFu;
+    // segments the batch's slots use: 0..seg_max (bit 31: any segment >= 31)
+    s_act = ctl->seg_max >= 31u ? 0xFFFFFFFFu : ((2u << ctl->seg_max) - 1u);
     s_inc = batch_counts && batch_counts[k] > 0;
     if (blockIdx.x == 0) {
       ctl->ctr[0] += 1;
@@ -402,7 +404,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
     // push cannot change it
     lit = (m.x & s_need) == s_need && !(m.y >> 31);
     if (LEARN) {
-      if ((m.x | (m.y & 0x7FFFFFFFu)) != 0u) fan = __ldg(L.inv_off + i + 1) - __ldg(L.inv_off + i);
+      // active: some head covers a segment that a slot of the batch uses
+      if (((m.x | (m.y & 0x7FFFFFFFu)) & s_act) != 0u) fan = __ldg(L.inv_off + i + 1) - __ldg(L.inv_off + i);
 #pragma unroll
       for (int j = 0; j < 8; j++) inflight += h[j] < 255u + s_pmax ? 1u : 0u;
     }

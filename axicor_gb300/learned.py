@@ -31,7 +31,7 @@ def param_count() -> int:
 @dataclass
 class Policy:
     policy: int = -1          # -1 predictor, 0 always dense, 1 always sparse (exact buffers)
-    ratio: float = 4.0
+    ratio: float = 3.0
     margin: float = 0.25
     slack: int = 64
 

@@ -34,6 +34,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 CONFIGS = {"plain-1.5M": "config1", "plain-16k": "config0", "plain-8M": "config4"}
+# learned-schedule workloads: the 1.5M brain as configured (saturated dynamics),
+# and the same brain with homeostasis on and the 0.01..0.2 sinusoidal input (quiet)
+LEARNED = {"learned-1.5M": False, "learned-homeostatic-1.5M": True}
 
 
 def parse():
@@ -42,7 +45,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="plain-1.5M", choices=sorted(CONFIGS) + ["population-512"])
+    ap.add_argument("--workload", default="plain-1.5M",
+                    choices=sorted(CONFIGS) + ["population-512"] + sorted(LEARNED))
+    ap.add_argument("--learned-ticks", type=int, default=10000)
+    ap.add_argument("--learned-epochs", type=int, default=30)
+    ap.add_argument("--learned-ratio", type=float, default=3.0)
     ap.add_argument("--pop-brains", type=int, default=512)
     ap.add_argument("--pop-ticks", type=int, default=2000)
     ap.add_argument("--ticks-per-step", type=int, default=100)
@@ -470,10 +477,143 @@ def run_population(args) -> None:
         b.free()
 
 
+def run_learned(args) -> None:
+    """The learned schedule against the plain path on the same brain and ticks.
+
+    Ticks [0, trace): dense with trace recording (200k tile-ticks), then GPU
+    training; [trace, trace+200): the predictor running but forced dense (its
+    overhead); [trace+200, total): the predictor's schedule.  The plain copy
+    of the brain runs the same ticks through axc_step_day_phase_batch; final
+    states are compared."""
+    import hashlib
+    import torch
+    import __graft_entry__ as G
+    G.build()
+    from axicor_gb300 import _native as N
+    from axicor_gb300 import learned as L
+    from axicor_gb300 import shard as S
+    from axicor_gb300 import workloads as W
+    lib = N.lib()
+    lib.gpu_set_device(0)
+    w = W.config1()
+    if LEARNED[args.workload]:
+        w = W.homeostatic(w)
+    tpg = args.ticks_per_step
+    total = args.learned_ticks
+    lay, state, heads = S.generate_brain(w.spec())
+    synapses = synapse_count(state, lay.padded_n)
+    S.upload_lut(w.lut)
+    words = max((w.num_inputs + 31) // 32, 1)
+    bm = S.input_bitmask(w.seed, 0, total, w.num_inputs, w.rate_q32)
+    d_bm = S.device_array(bm)
+    tiles = (lay.total_axons + 1023) // 1024
+    samples_cap = 200_000
+    trace = -(-(samples_cap // tiles + 2) // tpg) * tpg
+    window = 2 * tpg
+    assert total > trace + window and (total - trace - window) % tpg == 0
+    vl = S.VramState(lay.padded_n, lay.total_axons)
+    vp = S.VramState(lay.padded_n, lay.total_axons)
+    for v in (vl, vp):
+        v.upload_state(state)
+        v.upload_axon_heads(heads)
+    eng = L.LearnedEngine(vl, lay.padded_n, lay.total_axons, lay.virtual_offset, w.num_inputs, d_bm, words, total,
+                          w.v_seg, w.dopamine, 0, samples_cap)
+    plain = S.ShardEngine(vp)
+    io = S.IoDeviceBuffers(words, 0, 0, tpg)
+    ps = torch.cuda.ExternalStream(plain.stream)
+
+    def plain_run(t0, ticks):
+        for t in range(t0, t0 + ticks, tpg):
+            err = lib.axc_step_day_phase_batch(C.byref(vp.ptrs), lay.padded_n, lay.total_axons, tpg,
+                                               C.byref(io.as_struct()), d_bm + t * words * 4, None, None,
+                                               lay.virtual_offset, w.num_inputs, None, w.v_seg, w.dopamine, t,
+                                               None, plain.stream)
+            assert err == 0, err
+
+    def timed(fn, stream):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    # 1. traces (dense ticks) and training
+    eng.set_policy(L.Policy(policy=0))
+    eng.collect(True, reset=True)
+    eng.run(0, trace, tpg)
+    eng.collect(False)
+    plain_run(0, trace)
+    torch.cuda.synchronize()
+    n_samples = eng.stats()["samples"]
+    t0 = time.perf_counter()
+    loss, val = eng.train(epochs=args.learned_epochs, batch=1024, lr=2e-3, seed=7)
+    train_s = time.perf_counter() - t0
+    default = torch.cuda.default_stream()
+    # 2. the predictor's overhead: features + inference + plan, schedule forced dense
+    eng.set_policy(L.Policy(policy=-1, ratio=float("inf")))
+    t_over = timed(lambda: eng.run(trace, window, tpg), default)
+    t_plain_w = timed(lambda: plain_run(trace, window), ps)
+    # 3. the learned schedule
+    eng.set_policy(L.Policy(policy=-1, ratio=args.learned_ratio))
+    eng.reset_stats()
+    t1 = trace + window
+    ticks = total - t1
+    clocks = Clocks(0)
+    clocks.start()
+    t_learned = timed(lambda: eng.run(t1, ticks, tpg), default)
+    t_plain = timed(lambda: plain_run(t1, ticks), ps)
+    clk = clocks.stop()
+    st = eng.stats()
+
+    def digest(v):
+        h = hashlib.sha256()
+        h.update(v.download_state().tobytes())
+        h.update(v.download_heads().tobytes())
+        return h.hexdigest()
+
+    same = digest(vl) == digest(vp)
+    tps_l, tps_p = ticks / t_learned, ticks / t_plain
+    ctr = vl.counters()
+    line = {
+        "metric": "synaptic_events_per_s", "value": tps_l * synapses, "unit": "events/s", "n_gpus": 1,
+        "steps": ticks // tpg, "warmup": t1 // tpg, "ms_per_step": t_learned * 1e3 / (ticks // tpg),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator, inputs resident in HBM)", "ticks_per_s": tps_l,
+        "config": {"workload": args.workload, "neurons": lay.padded_n, "synapses": synapses, "ticks": total,
+                   "timed_ticks": ticks, "trace_ticks": trace, "tiles": tiles, "samples": n_samples,
+                   "epochs": args.learned_epochs, "ratio": args.learned_ratio, "ticks_per_step": tpg},
+        "plain": {"value": tps_p * synapses, "unit": "events/s", "ticks_per_s": tps_p,
+                  "how": "the same brain and ticks through axc_step_day_phase_batch (row engine)"},
+        "speedup_vs_plain": t_plain / t_learned,
+        "bitexact_vs_plain": same,
+        "predictor": {
+            "sparse_ticks": st["sparse_ticks"], "planned_sparse": st["planned_sparse"],
+            "overflow_reruns": st["overflow_reruns"],
+            "misprediction_rate": st["overflow_reruns"] / max(st["planned_sparse"], 1),
+            "schedule_mismatch_rate": st["schedule_mismatches"] / max(st["judged_ticks"], 1),
+            "mean_abs_err_frac": st["abs_err_synapses"] / max(st["actual_synapses"], 1),
+            "overhead_us_per_tick": (t_over - t_plain_w) / window * 1e6,
+            "overhead_frac": (t_over - t_plain_w) / t_plain_w,
+            "train_s": train_s, "train_loss_first": loss[0] if loss else None,
+            "train_loss_last": loss[-1] if loss else None, "val_mse": val,
+        },
+        "per_tick": {"evaluated_slots": float(ctr[1]) / total, "hits": float(ctr[2]) / total,
+                     "spikes": float(ctr[3]) / total},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
 def main():
     args = parse()
     if args.workload.startswith("population"):
         run_population(args)
+        return
+    if args.workload in LEARNED:
+        run_learned(args)
         return
     dist = Dist(args.gpus)
     try:
