@@ -130,102 +130,98 @@ __device__ void block_scan_1024(const uint32_t* cnt, uint32_t* out, uint32_t n) 
   __syncthreads();
 }
 
+// Capacity (synapses) of tile j's compaction segment on a sparse tick.
+__device__ __forceinline__ uint32_t tile_cap(const LearnCtl& c, float pred, uint32_t fan) {
+  if (c.policy == 1) return fan;
+  const float want = fmaxf(pred, 0.f) * (float)fan * (1.f + c.margin) + (float)c.slack;
+  return want >= (float)fan ? fan : (uint32_t)want;
+}
+
+// The schedule of the next tick, by one thread, from totals over the tiles:
+// ty / terr the finished tick's active synapses and prediction error (when
+// the features kernel ran), tp the predicted active synapses and tnext the
+// evaluated slots of the next tick, rate its input spike fraction.
+__device__ void plan_serial(LearnCtl& c, const ShardCtl* sc, unsigned long long ty, unsigned long long terr,
+                            unsigned long long tp, unsigned long long tnext, float rate, bool features_ran) {
+  if (c.prev_learned && features_ran) {   // the finished tick, judged with exact counts
+    const bool best_sparse = c.ratio * (float)ty < (float)c.eval_now;
+    if (best_sparse != (c.prev_mode == 1u)) c.stat[kStMismatch]++;
+    c.stat[kStJudged]++;
+    c.stat[kStAbsErr] += terr;
+    c.stat[kStActual] += ty;
+  }
+  if (features_ran) {
+    if (c.collect && c.ticks_seen >= 1 && (c.ticks_seen % c.sample_every) == 0 && c.samples + c.T <= c.sample_cap)
+      c.samples += c.T;
+    c.ticks_seen++;
+  } else {
+    c.ticks_seen = 0;   // the feature history restarts
+  }
+  for (int q = 8; q > 0; q--) c.inrate[q] = c.inrate[q - 1];
+  c.inrate[0] = rate;
+  c.stale = (sc->row_sum != c.row_sum) ? 1u : 0u;
+  const bool learned = features_ran && c.policy < 0 && c.ticks_seen > 0 && !c.stale;
+  bool sparse;
+  if (c.stale) sparse = false;
+  else if (c.policy == 1) sparse = true;
+  else sparse = learned && c.ratio * (float)tp < (float)tnext;
+  c.pred_total = (float)tp;
+  c.eval_now = tnext;
+  c.mode = sparse ? 1u : 0u;
+  c.prev_mode = c.mode;
+  c.prev_learned = learned ? 1u : 0u;
+  c.overflow = 0;
+  c.spk_count = 0;
+}
+
 // ---------------------------------------------------------------------------
-// per tick 0: the schedule.  One block of 1024 threads.
+// per tick 0: the schedule.  When the features kernel's last block already
+// planned this tick, only the targets checksum is re-checked (the row copy at
+// the start of a graph recomputes it).  Otherwise (first tick of a feature
+// history, or a graph without features): one block of 1024 threads plans from
+// the tile arrays.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __restrict__ pred,
-                                                     const uint32_t* __restrict__ fan,
-                                                     const uint32_t* __restrict__ axn, uint32_t* __restrict__ cap,
-                                                     uint32_t* __restrict__ seg, uint32_t* __restrict__ entries,
+                                                     const uint32_t* __restrict__ fan, uint32_t* __restrict__ cap,
                                                      const uint32_t* __restrict__ bits, uint32_t words, uint32_t nv,
-                                                     const ShardCtl* __restrict__ sc, uint32_t features_on) {
+                                                     const ShardCtl* __restrict__ sc) {
   LearnCtl& c = *L.ctl;
-  const uint32_t T = c.T;
-  __shared__ float s_pf[32];
-  __shared__ unsigned long long s_y[32];
-  __shared__ uint32_t s_in[32];
-  __shared__ uint32_t s_sparse;
-  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // the previous tick, judged with exact counts: its total active synapses
-  // (still in yacc) and its evaluated slots
-  unsigned long long y = 0;
-  float pf = 0.f;
-  for (uint32_t j = threadIdx.x; j < T; j += 1024) {
-    y += L.yacc[j];
-    pf += fmaxf(pred[j], 0.f) * (float)fan[j];
+  if (c.planned) {
+    if (threadIdx.x == 0) {
+      c.planned = 0;
+      if (sc->row_sum != c.row_sum && !c.stale) {
+        c.stale = 1u;
+        c.mode = 0u;
+        c.prev_mode = 0u;
+        c.prev_learned = 0u;
+      }
+    }
+    return;
   }
+  const uint32_t T = c.T;
+  __shared__ uint32_t s_in[32];
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t ib = 0;
   for (uint32_t q = threadIdx.x; q < words; q += 1024) {
     uint32_t x = bits ? bits[q] : 0u;
     if (32u * q + 32u > nv) x &= (32u * q >= nv) ? 0u : ((1u << (nv - 32u * q)) - 1u);
     ib += __popc(x);
   }
-  y = warp_sum(y);
-  pf = warp_sum_f(pf);
   ib = warp_sum(ib);
-  if (lane == 0) { s_y[w] = y; s_pf[w] = pf; s_in[w] = ib; }
+  if (lane == 0) s_in[w] = ib;
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long ty = 0;
-    float tp = 0.f;
     uint32_t ti = 0;
-    for (int q = 0; q < 32; q++) { ty += s_y[q]; tp += s_pf[q]; ti += s_in[q]; }
-    // the previous tick, judged with exact counts when the predictor chose its schedule
-    if (c.prev_learned) {
-      const bool best_sparse = c.ratio * (float)ty < (float)c.eval_now;
-      if (best_sparse != (c.prev_mode == 1u)) c.stat[kStMismatch]++;
-      c.stat[kStJudged]++;
-    }
-    if (c.feat_done) {       // the features kernel completed the previous tick
-      if (c.collect && c.ticks_seen >= 1 && (c.ticks_seen % c.sample_every) == 0 && c.samples + T <= c.sample_cap)
-        c.samples += T;
-      c.ticks_seen++;
-      c.feat_done = 0;
-    } else {
-      c.ticks_seen = 0;      // the feature history restarts
-    }
-    for (int q = 8; q > 0; q--) c.inrate[q] = c.inrate[q - 1];
-    c.inrate[0] = nv ? (float)ti / (float)nv : 0.f;
-    c.stale = (sc->row_sum != c.row_sum) ? 1u : 0u;
-    const bool learned = features_on && c.policy < 0 && c.ticks_seen > 0 && !c.stale;
-    bool sparse;
-    if (c.stale) sparse = false;
-    else if (c.policy == 1) sparse = true;
-    else sparse = learned && c.ratio * tp < (float)c.eval_next;
-    if (c.stale) c.stat[kStStale]++;
-    c.stat[kStTicks]++;
-    if (sparse) c.stat[kStSparsePicked]++;
-    c.prev_learned = learned ? 1u : 0u;
-    c.pred_total = tp;
-    c.eval_now = c.eval_next;
-    c.eval_next = 0;
-    c.mode = sparse ? 1u : 0u;
-    c.prev_mode = c.mode;
-    c.overflow = 0;
-    c.spk_count = 0;
-    s_sparse = sparse ? 1u : 0u;
+    for (int q = 0; q < 32; q++) ti += s_in[q];
+    plan_serial(c, sc, 0, 0, 0, 0, nv ? (float)ti / (float)nv : 0.f, false);
   }
   __syncthreads();
-  const bool sparse = s_sparse != 0u;
-  const bool exact = c.policy == 1;
   for (uint32_t j = threadIdx.x; j < T; j += 1024) {
-    uint32_t cp = 0;
-    if (sparse) {
-      if (exact) {
-        cp = fan[j];
-      } else {
-        const float want = fmaxf(pred[j], 0.f) * (float)fan[j] * (1.f + c.margin) + (float)c.slack;
-        cp = want >= (float)fan[j] ? fan[j] : (uint32_t)want;
-      }
-    }
-    cap[j] = cp;
-    entries[j] = min(cp, axn[j]);
+    cap[j] = tile_cap(c, pred[j], fan[j]);
     L.yacc[j] = 0;
     L.bacc[j] = 0;
     L.fill[j] = 0;
   }
-  __syncthreads();
-  block_scan_1024(entries, seg, T);
 }
 
 // ---------------------------------------------------------------------------
@@ -241,7 +237,14 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
                                                        const BurstHeads8* __restrict__ heads, uint32_t A,
                                                        int32_t* __restrict__ acc, ShardCtl* __restrict__ sc) {
   LearnCtl& c = *L.ctl;
-  if (blockIdx.x == 0 && threadIdx.x == 0 && c.mode == 1u) c.stat[c.overflow ? kStOverflow : kStSparse]++;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {   // accounting of the tick that runs
+    c.stat[kStTicks]++;
+    if (c.stale) c.stat[kStStale]++;
+    if (c.mode == 1u) {
+      c.stat[kStSparsePicked]++;
+      c.stat[c.overflow ? kStOverflow : kStSparse]++;
+    }
+  }
   if (c.mode != 1u || c.overflow) return;
   __shared__ uint32_t s_prop[16];
   __shared__ uint32_t s_pmax;
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
     const uint32_t b0 = threadIdx.x * per;
     uint32_t t = 0;
     for (uint32_t q = 0; q < per; q++)
-      if (b0 + q < T) t += min(L.fill[b0 + q], __ldg(L.seg + b0 + q + 1) - __ldg(L.seg + b0 + q));
+      if (b0 + q < T) t += L.fill[b0 + q];
     __shared__ uint32_t s_part[256];
     s_part[threadIdx.x] = t;
     __syncthreads();
@@ -269,7 +272,7 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
     for (uint32_t q = 0; q < per; q++)
       if (b0 + q < T) {
         s_pre[b0 + q] = run;
-        run += min(L.fill[b0 + q], __ldg(L.seg + b0 + q + 1) - __ldg(L.seg + b0 + q));
+        run += L.fill[b0 + q];
       }
     if (threadIdx.x == blockDim.x - 1) s_pre[T] = s_part[blockDim.x - 1];
     __syncthreads();
@@ -284,7 +287,7 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
       const uint32_t mid = (lo + hi) >> 1;
       if (s_pre[mid] <= e) lo = mid; else hi = mid;
     }
-    const uint32_t a = L.alist[__ldg(L.seg + lo) + (e - s_pre[lo])];
+    const uint32_t a = L.alist[(size_t)lo * kTileN + (e - s_pre[lo])];
     const uint2 m = __ldg(mask2 + a);
     const uint32_t r0 = __ldg(L.inv_off + a), r1 = __ldg(L.inv_off + a + 1);
     for (uint32_t r = r0 + lane; r < r1; r += 32) {
@@ -444,16 +447,21 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
                                                         const uint32_t* __restrict__ fan,
                                                         const uint32_t* __restrict__ axn, float* __restrict__ hist,
                                                         float* __restrict__ feat, float* __restrict__ pred,
+                                                        uint32_t* __restrict__ cap, uint32_t* __restrict__ part,
                                                         const __nv_bfloat16* __restrict__ wb, float* __restrict__ X,
                                                         float* __restrict__ Y, const uint32_t* __restrict__ bits_next,
-                                                        uint32_t words, uint32_t nv) {
+                                                        uint32_t words, uint32_t nv, const ShardCtl* __restrict__ sc) {
   LearnCtl& c = *L.ctl;
+  const uint32_t T = c.T;
   const uint32_t j = blockIdx.x;
   const uint32_t u = threadIdx.x, lane = u & 31, w = u >> 5;
   __shared__ uint32_t s_cnt[8][4];
   __shared__ float s_old[kHistF];
   __shared__ float xb[kFeat];
   __shared__ float red[4];
+  __shared__ unsigned long long s_tot[4][4];
+  __shared__ uint32_t s_last;
+  const bool seen = c.ticks_seen > 0;   // x of the previous tick is in feat[]
   // 1. the tile's neurons after the tick
   uint32_t spk = 0, nxt = 0, nslots = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, ib = 0;
   const uint32_t n0 = j * kTileN;
@@ -476,32 +484,27 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   const uint32_t vals[8] = {spk, nxt, nslots, t1, t2, t3, t4, ib};
 #pragma unroll
   for (int q = 0; q < 8; q++) {
-    const uint32_t s = warp_sum(vals[q]);
-    if (lane == 0) s_cnt[q][w] = s;
+    const uint32_t v = warp_sum(vals[q]);
+    if (lane == 0) s_cnt[q][w] = v;
   }
-  if (u < kHistF) s_old[u] = hist[(size_t)j * kHistF + u];
+  if (u < kHistF) s_old[u] = seen ? hist[(size_t)j * kHistF + u] : 0.f;
+  const uint32_t ya = L.yacc[j], ba = L.bacc[j];
+  const float pred_old = pred[j];
   __syncthreads();
   uint32_t tot[8];
 #pragma unroll
   for (int q = 0; q < 8; q++) tot[q] = s_cnt[q][0] + s_cnt[q][1] + s_cnt[q][2] + s_cnt[q][3];
   const float fj = (float)max(fan[j], 1u);
   const float aj = (float)max(axn[j], 1u);
-  const float y_now = (float)L.yacc[j] / fj;
+  const float y_now = (float)ya / fj;
   // 2. training pair (features of the previous tick, this tick's target)
-  const bool seen = c.ticks_seen > 0;
-  if (seen && c.collect && (c.ticks_seen % c.sample_every) == 0 && c.samples + c.T <= c.sample_cap) {
+  if (seen && c.collect && (c.ticks_seen % c.sample_every) == 0 && c.samples + T <= c.sample_cap) {
     const size_t row = (size_t)c.samples + j;
     if (u < kFeat) X[row * kFeat + u] = feat[(size_t)j * kFeat + u];
     if (u == 0) Y[row] = y_now;
   }
-  if (u == 0 && seen && c.policy < 0) {
-    const float err = fabsf(fmaxf(pred[j], 0.f) - y_now) * fj;
-    atomicAdd(&c.stat[kStAbsErr], (unsigned long long)(err + 0.5f));
-    atomicAdd(&c.stat[kStActual], (unsigned long long)L.yacc[j]);
-  }
-  if (u == 0) atomicAdd(&c.eval_next, (unsigned long long)tot[2]);
   // 3. history shift and the feature vector
-  const float cur[kHistCh] = {(float)tot[0] / (float)kTileN, y_now, (float)L.bacc[j] / (8.f * aj),
+  const float cur[kHistCh] = {(float)tot[0] / (float)kTileN, y_now, (float)ba / (8.f * aj),
                               s_old[kHistCh * kHistLen] / (float)kTileN};
   float x = 0.f;
   if (u < kHistCh * kHistLen) {
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   } else if (u == 48) {
     x = 1.f;
   }
-  __syncthreads();   // everyone has read s_old / feat before they are overwritten
+  __syncthreads();   // every read of feat[] / hist[] is done
   if (u < kHistCh * kHistLen) hist[(size_t)j * kHistF + u] = x;
   if (u == 0) hist[(size_t)j * kHistF + kHistCh * kHistLen] = (float)tot[1];
   if (u < kFeat) {
@@ -530,10 +533,45 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
     feat[(size_t)j * kFeat + u] = x;
   }
   __syncthreads();
-  // 4. the prediction for the next tick
+  // 4. the prediction for the next tick, its capacity, the tile's partial
+  //    totals; this tick's accumulators are cleared for the next
   const float y = mlp_block_forward(wb, xb, red, nullptr, nullptr);
-  if (u == 0) pred[j] = y;
-  if (j == 0 && u == 0) c.feat_done = 1u;
+  if (u == 0) {
+    pred[j] = y;
+    cap[j] = tile_cap(c, y, fan[j]);
+    const float err = (seen && c.policy < 0) ? fabsf(fmaxf(pred_old, 0.f) - y_now) * fj : 0.f;
+    part[j] = ya;
+    part[T + j] = (uint32_t)(err + 0.5f);
+    part[2 * T + j] = (uint32_t)fminf(fmaxf(y, 0.f) * fj, fj);
+    part[3 * T + j] = tot[2];
+    L.yacc[j] = 0;
+    L.bacc[j] = 0;
+    L.fill[j] = 0;
+  }
+  // 5. the last block to finish plans the next tick
+  __threadfence();
+  __syncthreads();
+  if (u == 0) s_last = atomicAdd(&c.blocks_done, 1u) == T - 1 ? 1u : 0u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  unsigned long long a[4] = {0, 0, 0, 0};
+  for (uint32_t q = u; q < T; q += 128)
+#pragma unroll
+    for (int k = 0; k < 4; k++) a[k] += __ldcg(part + (size_t)k * T + q);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const unsigned long long v = warp_sum(a[k]);
+    if (lane == 0) s_tot[k][w] = v;
+  }
+  __syncthreads();
+  if (u == 0) {
+    unsigned long long t[4];
+    for (int k = 0; k < 4; k++) t[k] = s_tot[k][0] + s_tot[k][1] + s_tot[k][2] + s_tot[k][3];
+    c.blocks_done = 0;
+    plan_serial(c, sc, t[0], t[1], t[2], t[3], nv ? (float)tot[7] / (float)nv : 0.f, true);
+    c.planned = 1u;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -621,6 +659,8 @@ __global__ void k_learn_index_done(LearnCtl* c, const ShardCtl* sc) {
   c->ticks_seen = 0;
   c->feat_done = 0;
   c->prev_learned = 0;
+  c->planned = 0;
+  c->blocks_done = 0;
   c->eval_next = 0;
   c->eval_now = 0;
   for (int q = 0; q < 9; q++) c->inrate[q] = 0.f;
@@ -763,7 +803,7 @@ struct Learned {
   void* base = nullptr;
   LearnCtl* ctl = nullptr;
   uint32_t *inv_off = nullptr, *fan = nullptr, *axn = nullptr, *yacc = nullptr, *bacc = nullptr, *fill = nullptr;
-  uint32_t *cap = nullptr, *seg = nullptr, *entries = nullptr, *alist = nullptr, *evbits = nullptr, *spk = nullptr;
+  uint32_t *cap = nullptr, *part = nullptr, *alist = nullptr, *evbits = nullptr, *spk = nullptr;
   uint32_t *deg = nullptr, *bsum = nullptr, *idx = nullptr;
   int32_t* acc = nullptr;
   float *hist = nullptr, *feat = nullptr, *pred = nullptr, *X = nullptr, *Y = nullptr;
@@ -791,7 +831,6 @@ struct Learned {
     d.bacc = bacc;
     d.fill = fill;
     d.cap = cap;
-    d.seg = seg;
     d.alist = alist;
     d.evbits = evbits;
     return d;
@@ -879,8 +918,7 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool fe
   const int sms = sm_count();
   const LearnDev D = L.dev();
   const uint32_t* bits_k = L.nv ? L.stage + (size_t)k * L.words : nullptr;
-  k_learn_plan<<<1, 1024, 0, st>>>(D, L.pred, L.fan, L.axn, L.cap, L.seg, L.entries, bits_k, L.words, L.nv, s.ctl,
-                                   features_on ? 1u : 0u);
+  k_learn_plan<<<1, 1024, 0, st>>>(D, L.pred, L.fan, L.cap, bits_k, L.words, L.nv, s.ctl);
   const uint32_t G = std::max(A, N);
   const uint32_t raise = (bits_k && ((uint64_t)L.voff + L.nv > A)) ? AXC_ERR_VIRTUAL_RANGE : 0u;
   if (G)
@@ -904,8 +942,9 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool fe
   k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
                                        nullptr, nullptr, 0, s.ctl, k);
   if (features_on && L.T)
-    k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.wb, L.X, L.Y,
-                                          L.nv ? L.stage + (size_t)(k + 1) * L.words : nullptr, L.words, L.nv);
+    k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.cap, L.part,
+                                          L.wb, L.X, L.Y, L.nv ? L.stage + (size_t)(k + 1) * L.words : nullptr,
+                                          L.words, L.nv, s.ctl);
   return cudaGetLastError();
 }
 
@@ -941,8 +980,8 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   const size_t o_ctl = take(sizeof(LearnCtl));
   const size_t o_off = take(((size_t)A + 1) * 4), o_fan = take((size_t)T * 4), o_axn = take((size_t)T * 4);
   const size_t o_yacc = take((size_t)T * 4), o_bacc = take((size_t)T * 4), o_fill = take((size_t)T * 4);
-  const size_t o_cap = take((size_t)T * 4), o_seg = take(((size_t)T + 1) * 4), o_ent = take((size_t)T * 4);
-  const size_t o_alist = take((size_t)A * 4), o_ev = take(((size_t)N / 32 + 2) * 4), o_spk = take((size_t)N * 4 + 4);
+  const size_t o_cap = take((size_t)T * 4), o_part = take((size_t)T * 16);
+  const size_t o_alist = take((size_t)T * kTileN * 4), o_ev = take(((size_t)N / 32 + 2) * 4), o_spk = take((size_t)N * 4 + 4);
   const size_t o_deg = take((size_t)A * 4), o_bsum = take(4097 * 4), o_idx = take((size_t)L->sample_cap * 4 + 4);
   const size_t o_acc = take((size_t)N * 4 + 4);
   const size_t o_hist = take((size_t)T * kHistF * 4), o_feat = take((size_t)T * kFeat * 4);
@@ -965,8 +1004,7 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   L->bacc = reinterpret_cast<uint32_t*>(b + o_bacc);
   L->fill = reinterpret_cast<uint32_t*>(b + o_fill);
   L->cap = reinterpret_cast<uint32_t*>(b + o_cap);
-  L->seg = reinterpret_cast<uint32_t*>(b + o_seg);
-  L->entries = reinterpret_cast<uint32_t*>(b + o_ent);
+  L->part = reinterpret_cast<uint32_t*>(b + o_part);
   L->alist = reinterpret_cast<uint32_t*>(b + o_alist);
   L->evbits = reinterpret_cast<uint32_t*>(b + o_ev);
   L->spk = reinterpret_cast<uint32_t*>(b + o_spk);
@@ -1038,6 +1076,7 @@ int32_t axc_learned_set_policy(void* handle, int32_t policy, float ratio, float 
   if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return (int32_t)e;
   hc.policy = policy;
+  hc.planned = 0;   // the next tick is planned under the new policy
   hc.ratio = ratio;
   hc.margin = margin;
   hc.slack = slack;
@@ -1053,6 +1092,7 @@ int32_t axc_learned_collect(void* handle, uint32_t enable, uint32_t sample_every
   if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return (int32_t)e;
   hc.collect = enable ? 1u : 0u;
+  hc.planned = 0;
   hc.sample_every = sample_every;
   if (reset) hc.samples = 0;
   L->collect = hc.collect;

@@ -165,8 +165,10 @@ struct LearnCtl {
   uint32_t T;             // tiles of 1024 axons (= neurons)
   uint32_t prev_mode;     // the previous tick's schedule
   uint32_t prev_learned;  // the previous tick's schedule came from the predictor
-  uint32_t feat_done;     // the features kernel ran after the previous tick
-  uint32_t pad0;
+  uint32_t feat_done;     // unused
+  uint32_t planned;       // the features kernel's last block planned the next tick
+  uint32_t blocks_done;   // features blocks finished this tick (last-block detection)
+  uint32_t pad0, pad1;
   unsigned long long eval_next;   // evaluated slots of the next tick (features kernel)
   unsigned long long eval_now;    // evaluated slots of this tick
   unsigned long long row_sum;     // targets checksum the inverted index was built from
@@ -182,8 +184,7 @@ struct LearnDev {
   uint32_t* bacc;           // [T] heads in flight on the tile's axons this tick
   uint32_t* fill;           // [T] axons compacted into the tile's segment
   const uint32_t* cap;      // [T] the tile's capacity in synapses
-  const uint32_t* seg;      // [T+1] segment offsets into alist
-  uint32_t* alist;          // active axons of a sparse tick
+  uint32_t* alist;          // active axons of a sparse tick, tile j at [1024 j, 1024 j + fill[j])
   uint32_t* evbits;         // [N/32+1] evaluated neurons of the tick
 };
 
@@ -302,7 +303,8 @@ __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ we
 // Learned engine, in the prologue: per-tile active synapses and heads in
 // flight; on a sparse tick, the block's active axons go into its tile's
 // segment (a 256-thread block lies inside one 1024-axon tile).  A tile whose
-// actual activity exceeds its capacity sets the overflow flag.
+// active synapses exceed the capacity the predictor gave it sets the overflow
+// flag.
 __device__ __forceinline__ void learn_axons(const LearnDev& L, uint32_t i, uint32_t A, uint32_t fan,
                                             uint32_t inflight) {
   __shared__ uint32_t s_red[3][8];
@@ -329,19 +331,15 @@ __device__ __forceinline__ void learn_axons(const LearnDev& L, uint32_t i, uint3
     if (i0 < A) {
       const uint32_t old = atomicAdd(&L.yacc[j], tf);
       atomicAdd(&L.bacc[j], tb);
-      if (sparse && tc) {
-        s_base2 = atomicAdd(&L.fill[j], tc);
-        if (old + tf > L.cap[j] || s_base2 + tc > L.seg[j + 1] - L.seg[j]) L.ctl->overflow = 1u;
-      } else if (sparse && old + tf > L.cap[j]) {
-        L.ctl->overflow = 1u;
+      if (sparse) {
+        if (tc) s_base2 = atomicAdd(&L.fill[j], tc);
+        if (old + tf > L.cap[j]) L.ctl->overflow = 1u;
       }
     }
   }
   __syncthreads();
-  if (sparse && act) {
-    const uint32_t pos = s_base2 + s_red[2][w] + __popc(ball & ((1u << lane) - 1u));
-    if (pos < L.seg[j + 1] - L.seg[j]) L.alist[L.seg[j] + pos] = i;
-  }
+  // an axon is appended once per tick, so a tile's segment never exceeds its 1024 axons
+  if (sparse && act) L.alist[(size_t)j * 1024u + s_base2 + s_red[2][w] + __popc(ball & ((1u << lane) - 1u))] = i;
 }
 
 // ---------------------------------------------------------------------------

@@ -175,8 +175,8 @@ def test_learned_schedule_faster_than_plain_on_quiet_brain(gpu):
     row pass, with the same final state."""
     warm, collect, ticks = 300, 200, 300
     total = warm + collect + ticks
-    w = W.homeostatic(W.small(dims=(64, 64, 32), slots=100, inputs=2048, p=0.05, ticks=total, seed=31))
-    b = LBrain(w, total, sample_capacity=200 * 130)
+    w = W.homeostatic(W.small(dims=(128, 64, 64), slots=100, inputs=4096, p=0.05, ticks=total, seed=31))
+    b = LBrain(w, total, sample_capacity=100_000)
     lay = b.lay
     plain = S.VramState(lay.padded_n, lay.total_axons)
     plain.upload_state(b.state0)
