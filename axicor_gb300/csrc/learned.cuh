@@ -141,7 +141,7 @@ __device__ __forceinline__ uint32_t tile_cap(const LearnCtl& c, float pred, uint
 // ty / terr the finished tick's active synapses and prediction error (when
 // the features kernel ran), tp the predicted active synapses and tnext the
 // evaluated slots of the next tick, rate its input spike fraction.
-__device__ void plan_serial(LearnCtl& c, const ShardCtl* sc, unsigned long long ty, unsigned long long terr,
+__device__ void plan_serial(LearnCtl& c, unsigned long long row_sum, unsigned long long ty, unsigned long long terr,
                             unsigned long long tp, unsigned long long tnext, float rate, bool features_ran) {
   if (c.prev_learned && features_ran) {   // the finished tick, judged with exact counts
     const bool best_sparse = c.ratio * (float)ty < (float)c.eval_now;
@@ -159,7 +159,7 @@ __device__ void plan_serial(LearnCtl& c, const ShardCtl* sc, unsigned long long 
   }
   for (int q = 8; q > 0; q--) c.inrate[q] = c.inrate[q - 1];
   c.inrate[0] = rate;
-  c.stale = (sc->row_sum != c.row_sum) ? 1u : 0u;
+  c.stale = (row_sum != c.row_sum) ? 1u : 0u;
   const bool learned = features_ran && c.policy < 0 && c.ticks_seen > 0 && !c.stale;
   bool sparse;
   if (c.stale) sparse = false;
@@ -172,6 +172,17 @@ __device__ void plan_serial(LearnCtl& c, const ShardCtl* sc, unsigned long long 
   c.prev_learned = learned ? 1u : 0u;
   c.overflow = 0;
   c.spk_count = 0;
+}
+
+// The control block is staged in shared memory around plan_serial, which
+// would otherwise be a chain of dependent global-memory accesses.
+__device__ __forceinline__ void ctl_load(LearnCtl* dst, const LearnCtl* src) {
+  for (uint32_t q = threadIdx.x; q < sizeof(LearnCtl) / 4; q += blockDim.x)
+    reinterpret_cast<uint32_t*>(dst)[q] = __ldcg(reinterpret_cast<const uint32_t*>(src) + q);
+}
+__device__ __forceinline__ void ctl_store(LearnCtl* dst, const LearnCtl* src) {
+  for (uint32_t q = threadIdx.x; q < sizeof(LearnCtl) / 4; q += blockDim.x)
+    reinterpret_cast<uint32_t*>(dst)[q] = reinterpret_cast<const uint32_t*>(src)[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -200,7 +211,9 @@ __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __
   }
   const uint32_t T = c.T;
   __shared__ uint32_t s_in[32];
+  __shared__ LearnCtl s_c;
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  ctl_load(&s_c, &c);
   uint32_t ib = 0;
   for (uint32_t q = threadIdx.x; q < words; q += 1024) {
     uint32_t x = bits ? bits[q] : 0u;
@@ -213,11 +226,12 @@ __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __
   if (threadIdx.x == 0) {
     uint32_t ti = 0;
     for (int q = 0; q < 32; q++) ti += s_in[q];
-    plan_serial(c, sc, 0, 0, 0, 0, nv ? (float)ti / (float)nv : 0.f, false);
+    plan_serial(s_c, sc->row_sum, 0, 0, 0, 0, nv ? (float)ti / (float)nv : 0.f, false);
   }
   __syncthreads();
+  ctl_store(&c, &s_c);
   for (uint32_t j = threadIdx.x; j < T; j += 1024) {
-    cap[j] = tile_cap(c, pred[j], fan[j]);
+    cap[j] = tile_cap(s_c, pred[j], fan[j]);
     L.yacc[j] = 0;
     L.bacc[j] = 0;
     L.fill[j] = 0;
@@ -461,6 +475,7 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   __shared__ float red[4];
   __shared__ unsigned long long s_tot[4][4];
   __shared__ uint32_t s_last;
+  __shared__ LearnCtl s_c;
   const bool seen = c.ticks_seen > 0;   // x of the previous tick is in feat[]
   // 1. the tile's neurons after the tick
   uint32_t spk = 0, nxt = 0, nslots = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, ib = 0;
@@ -564,14 +579,17 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
     const unsigned long long v = warp_sum(a[k]);
     if (lane == 0) s_tot[k][w] = v;
   }
+  ctl_load(&s_c, &c);
   __syncthreads();
   if (u == 0) {
     unsigned long long t[4];
     for (int k = 0; k < 4; k++) t[k] = s_tot[k][0] + s_tot[k][1] + s_tot[k][2] + s_tot[k][3];
-    c.blocks_done = 0;
-    plan_serial(c, sc, t[0], t[1], t[2], t[3], nv ? (float)tot[7] / (float)nv : 0.f, true);
-    c.planned = 1u;
+    s_c.blocks_done = 0;
+    plan_serial(s_c, sc->row_sum, t[0], t[1], t[2], t[3], nv ? (float)tot[7] / (float)nv : 0.f, true);
+    s_c.planned = 1u;
   }
+  __syncthreads();
+  ctl_store(&c, &s_c);
 }
 
 // ---------------------------------------------------------------------------

@@ -112,8 +112,7 @@ def test_predictor_collect_train_run_bit_exact(gpu):
         b.eng.run(0, 120, 20)
         b.eng.collect(False)
         st = b.eng.stats()
-        # pairs of ticks 1..118 are committed (a tick's pairs count once the next tick starts)
-        assert st["samples"] == st["tiles"] * 118
+        assert st["samples"] == st["tiles"] * 119            # pairs (x of tick t-1, y of tick t), t = 1..119
         x, y = b.eng.samples(0, st["samples"])
         assert np.all(np.isfinite(x)) and np.all((y >= 0) & (y <= 1))
         loss, val = b.eng.train(epochs=40, batch=256, lr=2e-3, seed=3)
