@@ -192,10 +192,20 @@ __device__ __forceinline__ void ctl_store(LearnCtl* dst, const LearnCtl* src) {
 // history, or a graph without features): one block of 1024 threads plans from
 // the tile arrays.
 // ---------------------------------------------------------------------------
+// Accounting of the tick about to run, and the branch of its conditional
+// graph node (1: sparse form, 0: dense form).
+__device__ __forceinline__ void plan_commit(LearnCtl& c, cudaGraphConditionalHandle cond, uint32_t use_cond) {
+  c.stat[kStTicks]++;
+  if (c.stale) c.stat[kStStale]++;
+  if (c.mode == 1u) c.stat[kStSparsePicked]++;
+  if (use_cond) cudaGraphSetConditional(cond, c.mode);
+}
+
 __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __restrict__ pred,
                                                      const uint32_t* __restrict__ fan, uint32_t* __restrict__ cap,
                                                      const uint32_t* __restrict__ bits, uint32_t words, uint32_t nv,
-                                                     const ShardCtl* __restrict__ sc) {
+                                                     const ShardCtl* __restrict__ sc, cudaGraphConditionalHandle cond,
+                                                     uint32_t use_cond) {
   LearnCtl& c = *L.ctl;
   if (c.planned) {
     if (threadIdx.x == 0) {
@@ -206,6 +216,7 @@ __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __
         c.prev_mode = 0u;
         c.prev_learned = 0u;
       }
+      plan_commit(c, cond, use_cond);
     }
     return;
   }
@@ -227,6 +238,7 @@ __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __
     uint32_t ti = 0;
     for (int q = 0; q < 32; q++) ti += s_in[q];
     plan_serial(s_c, sc->row_sum, 0, 0, 0, 0, nv ? (float)ti / (float)nv : 0.f, false);
+    plan_commit(s_c, cond, use_cond);
   }
   __syncthreads();
   ctl_store(&c, &s_c);
@@ -251,14 +263,7 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
                                                        const BurstHeads8* __restrict__ heads, uint32_t A,
                                                        int32_t* __restrict__ acc, ShardCtl* __restrict__ sc) {
   LearnCtl& c = *L.ctl;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {   // accounting of the tick that runs
-    c.stat[kStTicks]++;
-    if (c.stale) c.stat[kStStale]++;
-    if (c.mode == 1u) {
-      c.stat[kStSparsePicked]++;
-      c.stat[c.overflow ? kStOverflow : kStSparse]++;
-    }
-  }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && c.mode == 1u) c.stat[c.overflow ? kStOverflow : kStSparse]++;
   if (c.mode != 1u || c.overflow) return;
   __shared__ uint32_t s_prop[16];
   __shared__ uint32_t s_pmax;
@@ -461,7 +466,7 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
                                                         const uint32_t* __restrict__ fan,
                                                         const uint32_t* __restrict__ axn, float* __restrict__ hist,
                                                         float* __restrict__ feat, float* __restrict__ pred,
-                                                        uint32_t* __restrict__ cap, uint32_t* __restrict__ part,
+                                                        uint32_t* __restrict__ cap,
                                                         const __nv_bfloat16* __restrict__ wb, float* __restrict__ X,
                                                         float* __restrict__ Y, const uint32_t* __restrict__ bits_next,
                                                         uint32_t words, uint32_t nv, const ShardCtl* __restrict__ sc) {
@@ -473,19 +478,38 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   __shared__ float s_old[kHistF];
   __shared__ float xb[kFeat];
   __shared__ float red[4];
-  __shared__ unsigned long long s_tot[4][4];
   __shared__ uint32_t s_last;
   __shared__ LearnCtl s_c;
   const bool seen = c.ticks_seen > 0;   // x of the previous tick is in feat[]
-  // 1. the tile's neurons after the tick
+  // 1. the tile's neurons after the tick: 8 consecutive neurons per thread,
+  //    one vector load each of timers, flags and row counts when aligned
   uint32_t spk = 0, nxt = 0, nslots = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, ib = 0;
-  const uint32_t n0 = j * kTileN;
-  for (uint32_t q = u; q < kTileN; q += 128) {
-    const uint32_t n = n0 + q;
-    if (n >= N) break;
-    const uint32_t tm = P.timers[n];
-    spk += P.soma_flags[n] & 1u;
-    if (tm == 0) { nxt++; nslots += cnt[n] & 0xFFu; }
+  const uint32_t n8 = j * kTileN + 8u * u;
+  const bool vec = ((reinterpret_cast<uintptr_t>(P.timers) | reinterpret_cast<uintptr_t>(P.soma_flags)) & 7u) == 0 &&
+                   n8 + 8u <= N;
+  uint32_t tmw[2] = {0xFFFFFFFFu, 0xFFFFFFFFu}, flw[2] = {0, 0}, cw[4] = {0, 0, 0, 0};
+  if (vec) {
+    const uint2 tm8 = *reinterpret_cast<const uint2*>(P.timers + n8);
+    const uint2 fl8 = *reinterpret_cast<const uint2*>(P.soma_flags + n8);
+    const uint4 c8 = *reinterpret_cast<const uint4*>(cnt + n8);
+    tmw[0] = tm8.x; tmw[1] = tm8.y; flw[0] = fl8.x; flw[1] = fl8.y;
+    cw[0] = c8.x; cw[1] = c8.y; cw[2] = c8.z; cw[3] = c8.w;
+  } else {
+    for (int q = 0; q < 8; q++) {
+      const uint32_t n = n8 + q;
+      if (n >= N) break;
+      const uint32_t sh = 8 * (q & 3);
+      tmw[q >> 2] = (tmw[q >> 2] & ~(0xFFu << sh)) | ((uint32_t)P.timers[n] << sh);
+      flw[q >> 2] |= (uint32_t)P.soma_flags[n] << sh;
+      cw[q >> 1] |= (uint32_t)cnt[n] << (16 * (q & 1));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 8; q++) {   // neurons past N are skipped
+    const uint32_t tm = (tmw[q >> 2] >> (8 * (q & 3))) & 0xFFu;
+    if (n8 + q >= N) continue;
+    spk += (flw[q >> 2] >> (8 * (q & 3))) & 1u;
+    if (tm == 0) { nxt++; nslots += (cw[q >> 1] >> (16 * (q & 1))) & 0xFFu; }
     t1 += tm == 1;
     t2 += tm == 2;
     t3 += tm == 3;
@@ -555,10 +579,10 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
     pred[j] = y;
     cap[j] = tile_cap(c, y, fan[j]);
     const float err = (seen && c.policy < 0) ? fabsf(fmaxf(pred_old, 0.f) - y_now) * fj : 0.f;
-    part[j] = ya;
-    part[T + j] = (uint32_t)(err + 0.5f);
-    part[2 * T + j] = (uint32_t)fminf(fmaxf(y, 0.f) * fj, fj);
-    part[3 * T + j] = tot[2];
+    atomicAdd(&c.part[0], (unsigned long long)ya);
+    atomicAdd(&c.part[1], (unsigned long long)(uint32_t)(err + 0.5f));
+    atomicAdd(&c.part[2], (unsigned long long)(uint32_t)fminf(fmaxf(y, 0.f) * fj, fj));
+    atomicAdd(&c.part[3], (unsigned long long)tot[2]);
     L.yacc[j] = 0;
     L.bacc[j] = 0;
     L.fill[j] = 0;
@@ -570,20 +594,14 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  unsigned long long a[4] = {0, 0, 0, 0};
-  for (uint32_t q = u; q < T; q += 128)
-#pragma unroll
-    for (int k = 0; k < 4; k++) a[k] += __ldcg(part + (size_t)k * T + q);
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const unsigned long long v = warp_sum(a[k]);
-    if (lane == 0) s_tot[k][w] = v;
-  }
   ctl_load(&s_c, &c);
   __syncthreads();
   if (u == 0) {
     unsigned long long t[4];
-    for (int k = 0; k < 4; k++) t[k] = s_tot[k][0] + s_tot[k][1] + s_tot[k][2] + s_tot[k][3];
+    for (int k = 0; k < 4; k++) {
+      t[k] = s_c.part[k];
+      s_c.part[k] = 0;
+    }
     s_c.blocks_done = 0;
     plan_serial(s_c, sc->row_sum, t[0], t[1], t[2], t[3], nv ? (float)tot[7] / (float)nv : 0.f, true);
     s_c.planned = 1u;
@@ -821,7 +839,7 @@ struct Learned {
   void* base = nullptr;
   LearnCtl* ctl = nullptr;
   uint32_t *inv_off = nullptr, *fan = nullptr, *axn = nullptr, *yacc = nullptr, *bacc = nullptr, *fill = nullptr;
-  uint32_t *cap = nullptr, *part = nullptr, *alist = nullptr, *evbits = nullptr, *spk = nullptr;
+  uint32_t *cap = nullptr, *alist = nullptr, *evbits = nullptr, *spk = nullptr;
   uint32_t *deg = nullptr, *bsum = nullptr, *idx = nullptr;
   int32_t* acc = nullptr;
   float *hist = nullptr, *feat = nullptr, *pred = nullptr, *X = nullptr, *Y = nullptr;
@@ -840,6 +858,8 @@ struct Learned {
   const void* rows_base = nullptr;   // the row cache the graphs were captured with
   std::map<std::tuple<uint32_t, uint32_t>, cudaGraphExec_t> graphs;
   cudaStream_t capture = nullptr;
+  cudaStream_t aux = nullptr;     // records the bodies of the conditional nodes
+  bool use_cond = true;           // conditional graph nodes select the update form
 
   LearnDev dev() const {
     LearnDev d;
@@ -863,6 +883,7 @@ static void learned_free(Learned* L) {
   if (!L) return;
   L->drop_graphs();
   if (L->capture) cudaStreamDestroy(L->capture);
+  if (L->aux) cudaStreamDestroy(L->aux);
   void* ptrs[] = {L->base, L->inv, L->inv_seg, L->stage, L->partial};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -928,22 +949,13 @@ static cudaError_t learned_index(Learned& L, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// One tick: schedule, prologue, both update forms (one of them returns at
-// once), fix-up, push, features + prediction.
-static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool features_on, cudaStream_t st) {
+// The update forms of one tick.  sparse: the dense update (it runs only when
+// the sparse form overflowed) and the sparse kernels; dense: the dense update.
+static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, bool sparse, cudaStream_t st) {
   RowCache& r = *s.rows;
   const uint32_t N = L.N, A = L.A;
   const int sms = sm_count();
   const LearnDev D = L.dev();
-  const uint32_t* bits_k = L.nv ? L.stage + (size_t)k * L.words : nullptr;
-  k_learn_plan<<<1, 1024, 0, st>>>(D, L.pred, L.fan, L.cap, bits_k, L.words, L.nv, s.ctl);
-  const uint32_t G = std::max(A, N);
-  const uint32_t raise = (bits_k && ((uint64_t)L.voff + L.nv > A)) ? AXC_ERR_VIRTUAL_RANGE : 0u;
-  if (G)
-    k_rows_prologue<true><<<(G + 255) / 256, 256, 0, st>>>(L.v.axon_heads, A, L.v_seg, bits_k, L.voff,
-                                                           bits_k ? L.nv : 0u, s.incoming, nullptr, k, r.mask2,
-                                                           r.mult, L.v.soma_flags, L.v.timers, N, r.eval, s.ctl,
-                                                           raise, r.lit, D);
   const uint32_t fix_cap = kFixCap;
   const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
   if (lit_bytes <= lit_smem_limit())
@@ -952,15 +964,84 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool fe
   else
     k_rows_update<false><<<4 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                    s.ctl, k, fix_cap, r.lit, L.ctl);
-  k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw, L.v.soma_flags, L.v.axon_heads,
-                                           A, L.acc, s.ctl);
+  if (!sparse) return;
+  k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw,
+                                                                L.v.soma_flags, L.v.axon_heads, A, L.acc, s.ctl);
   k_learn_update<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, L.spk, s.ctl, k);
   k_learn_gsop<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.rt, r.rw, r.cnt, r.mask2, L.spk, r.fix, s.ctl, fix_cap);
+}
+
+// Adds an if/else conditional node after the capture's current dependencies
+// and records the two forms into its bodies.  Returns false (and leaves the
+// capture untouched) when the runtime refuses conditional nodes.
+static bool learned_cond_forms(Learned& L, ShardScratch& s, uint32_t k, cudaStream_t st,
+                               cudaGraphConditionalHandle cond) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return false;
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = cond;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 2;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &p) != cudaSuccess) return false;
+  cudaGraph_t bodies[2] = {p.conditional.phGraph_out[0], p.conditional.phGraph_out[1]};
+  for (int b = 0; b < 2; b++) {
+    if (cudaStreamBeginCaptureToGraph(L.aux, bodies[b], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
+        cudaSuccess)
+      return false;
+    learned_update_forms(L, s, k, b == 0, L.aux);
+    cudaGraph_t out = nullptr;
+    if (cudaStreamEndCapture(L.aux, &out) != cudaSuccess) return false;
+  }
+  return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+         cudaSuccess;
+}
+
+// One tick: schedule, prologue, the update form the schedule picked (a
+// conditional graph node, or both forms with the one not picked returning at
+// once), fix-up, push, features + prediction.
+static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool features_on, cudaStream_t st) {
+  RowCache& r = *s.rows;
+  const uint32_t N = L.N, A = L.A;
+  const int sms = sm_count();
+  const LearnDev D = L.dev();
+  const uint32_t* bits_k = L.nv ? L.stage + (size_t)k * L.words : nullptr;
+  cudaGraphConditionalHandle cond = 0;
+  bool use_cond = false;
+  if (L.use_cond) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusActive &&
+        cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault) == cudaSuccess)
+      use_cond = true;
+    else
+      cudaGetLastError();
+  }
+  k_learn_plan<<<1, 1024, 0, st>>>(D, L.pred, L.fan, L.cap, bits_k, L.words, L.nv, s.ctl, cond, use_cond ? 1u : 0u);
+  const uint32_t G = std::max(A, N);
+  const uint32_t raise = (bits_k && ((uint64_t)L.voff + L.nv > A)) ? AXC_ERR_VIRTUAL_RANGE : 0u;
+  if (G)
+    k_rows_prologue<true><<<(G + 255) / 256, 256, 0, st>>>(L.v.axon_heads, A, L.v_seg, bits_k, L.voff,
+                                                           bits_k ? L.nv : 0u, s.incoming, nullptr, k, r.mask2,
+                                                           r.mult, L.v.soma_flags, L.v.timers, N, r.eval, s.ctl,
+                                                           raise, r.lit, D);
+  if (use_cond) {
+    if (!learned_cond_forms(L, s, k, st, cond)) return cudaErrorNotSupported;
+  } else {
+    learned_update_forms(L, s, k, true, st);
+  }
   k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k);
   k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
                                        nullptr, nullptr, 0, s.ctl, k);
   if (features_on && L.T)
-    k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.cap, L.part,
+    k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.cap,
                                           L.wb, L.X, L.Y, L.nv ? L.stage + (size_t)(k + 1) * L.words : nullptr,
                                           L.words, L.nv, s.ctl);
   return cudaGetLastError();
@@ -998,7 +1079,7 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   const size_t o_ctl = take(sizeof(LearnCtl));
   const size_t o_off = take(((size_t)A + 1) * 4), o_fan = take((size_t)T * 4), o_axn = take((size_t)T * 4);
   const size_t o_yacc = take((size_t)T * 4), o_bacc = take((size_t)T * 4), o_fill = take((size_t)T * 4);
-  const size_t o_cap = take((size_t)T * 4), o_part = take((size_t)T * 16);
+  const size_t o_cap = take((size_t)T * 4);
   const size_t o_alist = take((size_t)T * kTileN * 4), o_ev = take(((size_t)N / 32 + 2) * 4), o_spk = take((size_t)N * 4 + 4);
   const size_t o_deg = take((size_t)A * 4), o_bsum = take(4097 * 4), o_idx = take((size_t)L->sample_cap * 4 + 4);
   const size_t o_acc = take((size_t)N * 4 + 4);
@@ -1022,7 +1103,6 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   L->bacc = reinterpret_cast<uint32_t*>(b + o_bacc);
   L->fill = reinterpret_cast<uint32_t*>(b + o_fill);
   L->cap = reinterpret_cast<uint32_t*>(b + o_cap);
-  L->part = reinterpret_cast<uint32_t*>(b + o_part);
   L->alist = reinterpret_cast<uint32_t*>(b + o_alist);
   L->evbits = reinterpret_cast<uint32_t*>(b + o_ev);
   L->spk = reinterpret_cast<uint32_t*>(b + o_spk);
@@ -1066,6 +1146,7 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->capture, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->aux, cudaStreamNonBlocking);
   if (e == cudaSuccess && ((size_t)T + 1) * 4 > 48 * 1024)
     e = cudaFuncSetAttribute(k_learn_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(((size_t)T + 1) * 4));
   if (e == cudaSuccess) e = learned_index(*L, nullptr);
@@ -1147,17 +1228,23 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   if (it != L->graphs.end()) {
     exec = it->second;
   } else {
-    e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return (int32_t)e;
-    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture);
-    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = learned_tick(*L, *s, k, features_on, L->capture);
-    if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
-    cudaGraph_t g = nullptr;
-    e = cudaStreamEndCapture(L->capture, &g);
-    if (le != cudaSuccess) e = le;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
-    if (g) cudaGraphDestroy(g);
-    if (e != cudaSuccess) return (int32_t)e;
+    for (int attempt = 0; attempt < 2; attempt++) {
+      e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return (int32_t)e;
+      cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture);
+      for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = learned_tick(*L, *s, k, features_on, L->capture);
+      if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
+      cudaGraph_t g = nullptr;
+      e = cudaStreamEndCapture(L->capture, &g);
+      if (le != cudaSuccess) e = le;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e == cudaSuccess) break;
+      cudaGetLastError();
+      exec = nullptr;
+      if (!L->use_cond) return (int32_t)e;
+      L->use_cond = false;   // no conditional nodes here: both forms, the other returning at once
+    }
     L->graphs[key] = exec;
   }
   for (uint32_t c = 0; c < ticks / tpg && e == cudaSuccess; c++) {

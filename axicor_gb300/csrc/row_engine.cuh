@@ -175,6 +175,7 @@ struct LearnCtl {
   float pred_total;               // sum of the tile predictions for this tick (synapses)
   float inrate[9];                // input spike fraction of ticks t, t-1, ..., t-8
   unsigned long long stat[12];
+  unsigned long long part[4];     // features blocks' totals: active synapses, |error|, predicted, next evaluated slots
 };
 
 struct LearnDev {
