@@ -186,68 +186,74 @@ __device__ __forceinline__ void ctl_store(LearnCtl* dst, const LearnCtl* src) {
 }
 
 // ---------------------------------------------------------------------------
-// per tick 0: the schedule.  When the features kernel's last block already
-// planned this tick, only the targets checksum is re-checked (the row copy at
-// the start of a graph recomputes it).  Otherwise (first tick of a feature
-// history, or a graph without features): one block of 1024 threads plans from
-// the tile arrays.
+// per tick 0: the schedule, by one block of 1024 threads, from the totals of
+// the features kernel's per-tile partials (when it ran after the previous
+// tick) on a shared-memory copy of the control block.
 // ---------------------------------------------------------------------------
-// Accounting of the tick about to run, and the branch of its conditional
-// graph node (1: sparse form, 0: dense form).
-__device__ __forceinline__ void plan_commit(LearnCtl& c, cudaGraphConditionalHandle cond, uint32_t use_cond) {
+// Accounting of the tick about to run.
+__device__ __forceinline__ void plan_commit(LearnCtl& c) {
   c.stat[kStTicks]++;
   if (c.stale) c.stat[kStStale]++;
   if (c.mode == 1u) c.stat[kStSparsePicked]++;
-  if (use_cond) cudaGraphSetConditional(cond, c.mode);
 }
 
 __global__ void __launch_bounds__(1024) k_learn_plan(LearnDev L, const float* __restrict__ pred,
                                                      const uint32_t* __restrict__ fan, uint32_t* __restrict__ cap,
+                                                     const uint32_t* __restrict__ part,
                                                      const uint32_t* __restrict__ bits, uint32_t words, uint32_t nv,
-                                                     const ShardCtl* __restrict__ sc, cudaGraphConditionalHandle cond,
-                                                     uint32_t use_cond) {
+                                                     const ShardCtl* __restrict__ sc) {
   LearnCtl& c = *L.ctl;
-  if (c.planned) {
-    if (threadIdx.x == 0) {
-      c.planned = 0;
-      if (sc->row_sum != c.row_sum && !c.stale) {
-        c.stale = 1u;
-        c.mode = 0u;
-        c.prev_mode = 0u;
-        c.prev_learned = 0u;
-      }
-      plan_commit(c, cond, use_cond);
-    }
-    return;
-  }
-  const uint32_t T = c.T;
+  __shared__ unsigned long long s_part[4][32];
   __shared__ uint32_t s_in[32];
   __shared__ LearnCtl s_c;
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   ctl_load(&s_c, &c);
+  __syncthreads();
+  const uint32_t T = s_c.T;
+  const bool feat = s_c.feat_done != 0u;   // the features kernel ran after the previous tick
+  // totals of the previous tick's features blocks, and this tick's input spikes
+  unsigned long long a[4] = {0, 0, 0, 0};
+  if (feat)
+    for (uint32_t j = threadIdx.x; j < T; j += 1024)
+#pragma unroll
+      for (int k = 0; k < 4; k++) a[k] += part[(size_t)k * T + j];
   uint32_t ib = 0;
   for (uint32_t q = threadIdx.x; q < words; q += 1024) {
     uint32_t x = bits ? bits[q] : 0u;
     if (32u * q + 32u > nv) x &= (32u * q >= nv) ? 0u : ((1u << (nv - 32u * q)) - 1u);
     ib += __popc(x);
   }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const unsigned long long v = warp_sum(a[k]);
+    if (lane == 0) s_part[k][w] = v;
+  }
   ib = warp_sum(ib);
   if (lane == 0) s_in[w] = ib;
   __syncthreads();
   if (threadIdx.x == 0) {
+    unsigned long long t[4] = {0, 0, 0, 0};
     uint32_t ti = 0;
-    for (int q = 0; q < 32; q++) ti += s_in[q];
-    plan_serial(s_c, sc->row_sum, 0, 0, 0, 0, nv ? (float)ti / (float)nv : 0.f, false);
-    plan_commit(s_c, cond, use_cond);
+    for (int q = 0; q < 32; q++) {
+      for (int k = 0; k < 4; k++) t[k] += s_part[k][q];
+      ti += s_in[q];
+    }
+    plan_serial(s_c, sc->row_sum, t[0], t[1], t[2], t[3], nv ? (float)ti / (float)nv : 0.f, feat);
+    s_c.feat_done = 0;
+    plan_commit(s_c);
   }
   __syncthreads();
   ctl_store(&c, &s_c);
-  for (uint32_t j = threadIdx.x; j < T; j += 1024) {
-    cap[j] = tile_cap(s_c, pred[j], fan[j]);
-    L.yacc[j] = 0;
-    L.bacc[j] = 0;
-    L.fill[j] = 0;
-  }
+  // tile capacities: the features kernel wrote them for the planned tick,
+  // except without features (no prediction) or with exact buffers
+  if (!feat || s_c.policy == 1)
+    for (uint32_t j = threadIdx.x; j < T; j += 1024) cap[j] = tile_cap(s_c, pred[j], fan[j]);
+  if (!feat)
+    for (uint32_t j = threadIdx.x; j < T; j += 1024) {
+      L.yacc[j] = 0;
+      L.bacc[j] = 0;
+      L.fill[j] = 0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -466,7 +472,7 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
                                                         const uint32_t* __restrict__ fan,
                                                         const uint32_t* __restrict__ axn, float* __restrict__ hist,
                                                         float* __restrict__ feat, float* __restrict__ pred,
-                                                        uint32_t* __restrict__ cap,
+                                                        uint32_t* __restrict__ cap, uint32_t* __restrict__ part,
                                                         const __nv_bfloat16* __restrict__ wb, float* __restrict__ X,
                                                         float* __restrict__ Y, const uint32_t* __restrict__ bits_next,
                                                         uint32_t words, uint32_t nv, const ShardCtl* __restrict__ sc) {
@@ -478,8 +484,6 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   __shared__ float s_old[kHistF];
   __shared__ float xb[kFeat];
   __shared__ float red[4];
-  __shared__ uint32_t s_last;
-  __shared__ LearnCtl s_c;
   const bool seen = c.ticks_seen > 0;   // x of the previous tick is in feat[]
   // 1. the tile's neurons after the tick: 8 consecutive neurons per thread,
   //    one vector load each of timers, flags and row counts when aligned
@@ -579,35 +583,15 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
     pred[j] = y;
     cap[j] = tile_cap(c, y, fan[j]);
     const float err = (seen && c.policy < 0) ? fabsf(fmaxf(pred_old, 0.f) - y_now) * fj : 0.f;
-    atomicAdd(&c.part[0], (unsigned long long)ya);
-    atomicAdd(&c.part[1], (unsigned long long)(uint32_t)(err + 0.5f));
-    atomicAdd(&c.part[2], (unsigned long long)(uint32_t)fminf(fmaxf(y, 0.f) * fj, fj));
-    atomicAdd(&c.part[3], (unsigned long long)tot[2]);
+    part[j] = ya;
+    part[T + j] = (uint32_t)(err + 0.5f);
+    part[2 * T + j] = (uint32_t)fminf(fmaxf(y, 0.f) * fj, fj);
+    part[3 * T + j] = tot[2];
     L.yacc[j] = 0;
     L.bacc[j] = 0;
     L.fill[j] = 0;
+    if (j == 0) c.feat_done = 1u;
   }
-  // 5. the last block to finish plans the next tick
-  __threadfence();
-  __syncthreads();
-  if (u == 0) s_last = atomicAdd(&c.blocks_done, 1u) == T - 1 ? 1u : 0u;
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  ctl_load(&s_c, &c);
-  __syncthreads();
-  if (u == 0) {
-    unsigned long long t[4];
-    for (int k = 0; k < 4; k++) {
-      t[k] = s_c.part[k];
-      s_c.part[k] = 0;
-    }
-    s_c.blocks_done = 0;
-    plan_serial(s_c, sc->row_sum, t[0], t[1], t[2], t[3], nv ? (float)tot[7] / (float)nv : 0.f, true);
-    s_c.planned = 1u;
-  }
-  __syncthreads();
-  ctl_store(&c, &s_c);
 }
 
 // ---------------------------------------------------------------------------
@@ -695,8 +679,6 @@ __global__ void k_learn_index_done(LearnCtl* c, const ShardCtl* sc) {
   c->ticks_seen = 0;
   c->feat_done = 0;
   c->prev_learned = 0;
-  c->planned = 0;
-  c->blocks_done = 0;
   c->eval_next = 0;
   c->eval_now = 0;
   for (int q = 0; q < 9; q++) c->inrate[q] = 0.f;
@@ -839,7 +821,7 @@ struct Learned {
   void* base = nullptr;
   LearnCtl* ctl = nullptr;
   uint32_t *inv_off = nullptr, *fan = nullptr, *axn = nullptr, *yacc = nullptr, *bacc = nullptr, *fill = nullptr;
-  uint32_t *cap = nullptr, *alist = nullptr, *evbits = nullptr, *spk = nullptr;
+  uint32_t *cap = nullptr, *part = nullptr, *alist = nullptr, *evbits = nullptr, *spk = nullptr;
   uint32_t *deg = nullptr, *bsum = nullptr, *idx = nullptr;
   int32_t* acc = nullptr;
   float *hist = nullptr, *feat = nullptr, *pred = nullptr, *X = nullptr, *Y = nullptr;
@@ -858,8 +840,6 @@ struct Learned {
   const void* rows_base = nullptr;   // the row cache the graphs were captured with
   std::map<std::tuple<uint32_t, uint32_t>, cudaGraphExec_t> graphs;
   cudaStream_t capture = nullptr;
-  cudaStream_t aux = nullptr;     // records the bodies of the conditional nodes
-  bool use_cond = true;           // conditional graph nodes select the update form
 
   LearnDev dev() const {
     LearnDev d;
@@ -883,7 +863,6 @@ static void learned_free(Learned* L) {
   if (!L) return;
   L->drop_graphs();
   if (L->capture) cudaStreamDestroy(L->capture);
-  if (L->aux) cudaStreamDestroy(L->aux);
   void* ptrs[] = {L->base, L->inv, L->inv_seg, L->stage, L->partial};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -949,9 +928,10 @@ static cudaError_t learned_index(Learned& L, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// The update forms of one tick.  sparse: the dense update (it runs only when
-// the sparse form overflowed) and the sparse kernels; dense: the dense update.
-static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, bool sparse, cudaStream_t st) {
+// The update forms of one tick: the dense update (it returns at once on a
+// sparse tick that did not overflow) and the sparse kernels (they return at
+// once on a dense tick).
+static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, cudaStream_t st) {
   RowCache& r = *s.rows;
   const uint32_t N = L.N, A = L.A;
   const int sms = sm_count();
@@ -964,67 +944,21 @@ static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, bool s
   else
     k_rows_update<false><<<4 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                    s.ctl, k, fix_cap, r.lit, L.ctl);
-  if (!sparse) return;
   k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw,
                                                                 L.v.soma_flags, L.v.axon_heads, A, L.acc, s.ctl);
   k_learn_update<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, L.spk, s.ctl, k);
   k_learn_gsop<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.rt, r.rw, r.cnt, r.mask2, L.spk, r.fix, s.ctl, fix_cap);
 }
 
-// Adds an if/else conditional node after the capture's current dependencies
-// and records the two forms into its bodies.  Returns false (and leaves the
-// capture untouched) when the runtime refuses conditional nodes.
-static bool learned_cond_forms(Learned& L, ShardScratch& s, uint32_t k, cudaStream_t st,
-                               cudaGraphConditionalHandle cond) {
-  cudaStreamCaptureStatus cs;
-  cudaGraph_t g = nullptr;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t nd = 0;
-  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
-      cs != cudaStreamCaptureStatusActive)
-    return false;
-  cudaGraphNodeParams p{};
-  p.type = cudaGraphNodeTypeConditional;
-  p.conditional.handle = cond;
-  p.conditional.type = cudaGraphCondTypeIf;
-  p.conditional.size = 2;
-  cudaGraphNode_t node;
-  if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &p) != cudaSuccess) return false;
-  cudaGraph_t bodies[2] = {p.conditional.phGraph_out[0], p.conditional.phGraph_out[1]};
-  for (int b = 0; b < 2; b++) {
-    if (cudaStreamBeginCaptureToGraph(L.aux, bodies[b], nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
-        cudaSuccess)
-      return false;
-    learned_update_forms(L, s, k, b == 0, L.aux);
-    cudaGraph_t out = nullptr;
-    if (cudaStreamEndCapture(L.aux, &out) != cudaSuccess) return false;
-  }
-  return cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) ==
-         cudaSuccess;
-}
-
-// One tick: schedule, prologue, the update form the schedule picked (a
-// conditional graph node, or both forms with the one not picked returning at
-// once), fix-up, push, features + prediction.
+// One tick: schedule, prologue, both update forms (the one not picked returns
+// at once), fix-up, push, features + prediction.
 static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool features_on, cudaStream_t st) {
   RowCache& r = *s.rows;
   const uint32_t N = L.N, A = L.A;
   const int sms = sm_count();
   const LearnDev D = L.dev();
   const uint32_t* bits_k = L.nv ? L.stage + (size_t)k * L.words : nullptr;
-  cudaGraphConditionalHandle cond = 0;
-  bool use_cond = false;
-  if (L.use_cond) {
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t g = nullptr;
-    if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr) == cudaSuccess &&
-        cs == cudaStreamCaptureStatusActive &&
-        cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault) == cudaSuccess)
-      use_cond = true;
-    else
-      cudaGetLastError();
-  }
-  k_learn_plan<<<1, 1024, 0, st>>>(D, L.pred, L.fan, L.cap, bits_k, L.words, L.nv, s.ctl, cond, use_cond ? 1u : 0u);
+  k_learn_plan<<<1, 1024, 0, st>>>(D, L.pred, L.fan, L.cap, L.part, bits_k, L.words, L.nv, s.ctl);
   const uint32_t G = std::max(A, N);
   const uint32_t raise = (bits_k && ((uint64_t)L.voff + L.nv > A)) ? AXC_ERR_VIRTUAL_RANGE : 0u;
   if (G)
@@ -1032,16 +966,12 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool fe
                                                            bits_k ? L.nv : 0u, s.incoming, nullptr, k, r.mask2,
                                                            r.mult, L.v.soma_flags, L.v.timers, N, r.eval, s.ctl,
                                                            raise, r.lit, D);
-  if (use_cond) {
-    if (!learned_cond_forms(L, s, k, st, cond)) return cudaErrorNotSupported;
-  } else {
-    learned_update_forms(L, s, k, true, st);
-  }
+  learned_update_forms(L, s, k, st);
   k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k);
   k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
                                        nullptr, nullptr, 0, s.ctl, k);
   if (features_on && L.T)
-    k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.cap,
+    k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.cap, L.part,
                                           L.wb, L.X, L.Y, L.nv ? L.stage + (size_t)(k + 1) * L.words : nullptr,
                                           L.words, L.nv, s.ctl);
   return cudaGetLastError();
@@ -1079,7 +1009,7 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   const size_t o_ctl = take(sizeof(LearnCtl));
   const size_t o_off = take(((size_t)A + 1) * 4), o_fan = take((size_t)T * 4), o_axn = take((size_t)T * 4);
   const size_t o_yacc = take((size_t)T * 4), o_bacc = take((size_t)T * 4), o_fill = take((size_t)T * 4);
-  const size_t o_cap = take((size_t)T * 4);
+  const size_t o_cap = take((size_t)T * 4), o_part = take((size_t)T * 16);
   const size_t o_alist = take((size_t)T * kTileN * 4), o_ev = take(((size_t)N / 32 + 2) * 4), o_spk = take((size_t)N * 4 + 4);
   const size_t o_deg = take((size_t)A * 4), o_bsum = take(4097 * 4), o_idx = take((size_t)L->sample_cap * 4 + 4);
   const size_t o_acc = take((size_t)N * 4 + 4);
@@ -1103,6 +1033,7 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   L->bacc = reinterpret_cast<uint32_t*>(b + o_bacc);
   L->fill = reinterpret_cast<uint32_t*>(b + o_fill);
   L->cap = reinterpret_cast<uint32_t*>(b + o_cap);
+  L->part = reinterpret_cast<uint32_t*>(b + o_part);
   L->alist = reinterpret_cast<uint32_t*>(b + o_alist);
   L->evbits = reinterpret_cast<uint32_t*>(b + o_ev);
   L->spk = reinterpret_cast<uint32_t*>(b + o_spk);
@@ -1146,7 +1077,6 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->capture, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->aux, cudaStreamNonBlocking);
   if (e == cudaSuccess && ((size_t)T + 1) * 4 > 48 * 1024)
     e = cudaFuncSetAttribute(k_learn_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(((size_t)T + 1) * 4));
   if (e == cudaSuccess) e = learned_index(*L, nullptr);
@@ -1175,7 +1105,6 @@ int32_t axc_learned_set_policy(void* handle, int32_t policy, float ratio, float 
   if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return (int32_t)e;
   hc.policy = policy;
-  hc.planned = 0;   // the next tick is planned under the new policy
   hc.ratio = ratio;
   hc.margin = margin;
   hc.slack = slack;
@@ -1191,7 +1120,6 @@ int32_t axc_learned_collect(void* handle, uint32_t enable, uint32_t sample_every
   if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return (int32_t)e;
   hc.collect = enable ? 1u : 0u;
-  hc.planned = 0;
   hc.sample_every = sample_every;
   if (reset) hc.samples = 0;
   L->collect = hc.collect;
@@ -1228,23 +1156,17 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   if (it != L->graphs.end()) {
     exec = it->second;
   } else {
-    for (int attempt = 0; attempt < 2; attempt++) {
-      e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
-      if (e != cudaSuccess) return (int32_t)e;
-      cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture);
-      for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = learned_tick(*L, *s, k, features_on, L->capture);
-      if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
-      cudaGraph_t g = nullptr;
-      e = cudaStreamEndCapture(L->capture, &g);
-      if (le != cudaSuccess) e = le;
-      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
-      if (g) cudaGraphDestroy(g);
-      if (e == cudaSuccess) break;
-      cudaGetLastError();
-      exec = nullptr;
-      if (!L->use_cond) return (int32_t)e;
-      L->use_cond = false;   // no conditional nodes here: both forms, the other returning at once
-    }
+    e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return (int32_t)e;
+    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture);
+    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = learned_tick(*L, *s, k, features_on, L->capture);
+    if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(L->capture, &g);
+    if (le != cudaSuccess) e = le;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) return (int32_t)e;
     L->graphs[key] = exec;
   }
   for (uint32_t c = 0; c < ticks / tpg && e == cudaSuccess; c++) {

@@ -165,17 +165,14 @@ struct LearnCtl {
   uint32_t T;             // tiles of 1024 axons (= neurons)
   uint32_t prev_mode;     // the previous tick's schedule
   uint32_t prev_learned;  // the previous tick's schedule came from the predictor
-  uint32_t feat_done;     // unused
-  uint32_t planned;       // the features kernel's last block planned the next tick
-  uint32_t blocks_done;   // features blocks finished this tick (last-block detection)
-  uint32_t pad0, pad1;
+  uint32_t feat_done;     // the features kernel ran after the previous tick
+  uint32_t pad0, pad1, pad2, pad3;
   unsigned long long eval_next;   // evaluated slots of the next tick (features kernel)
   unsigned long long eval_now;    // evaluated slots of this tick
   unsigned long long row_sum;     // targets checksum the inverted index was built from
   float pred_total;               // sum of the tile predictions for this tick (synapses)
   float inrate[9];                // input spike fraction of ticks t, t-1, ..., t-8
   unsigned long long stat[12];
-  unsigned long long part[4];     // features blocks' totals: active synapses, |error|, predicted, next evaluated slots
 };
 
 struct LearnDev {
