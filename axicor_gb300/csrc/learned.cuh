@@ -1119,6 +1119,11 @@ int32_t axc_learned_collect(void* handle, uint32_t enable, uint32_t sample_every
   LearnCtl hc;
   if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return (int32_t)e;
+  // the pairs of the last tick collected are committed when the next tick is
+  // planned; switching collection off commits them here
+  if (hc.collect && !enable && hc.feat_done && hc.ticks_seen >= 1 && (hc.ticks_seen % hc.sample_every) == 0 &&
+      hc.samples + hc.T <= hc.sample_cap)
+    hc.samples += hc.T;
   hc.collect = enable ? 1u : 0u;
   hc.sample_every = sample_every;
   if (reset) hc.samples = 0;
