@@ -61,7 +61,9 @@ constexpr uint32_t kFixCap = 1u << 22;  // deferred GSOP slots per tick before t
 // Row engine (row_engine.cuh, compiled in day_phase.cu).
 cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix = true);
 void rows_free(ShardScratch& s);
-cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream);
+// row_sum: also compute the targets checksum (ShardCtl::row_sum) the learned engine checks its index against.
+cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
+                              bool row_sum = false);
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream);
 
 // Registry keyed by the axon_heads pointer.  Created by cu_allocate_shard;

@@ -887,7 +887,7 @@ static cudaError_t learned_index(Learned& L, cudaStream_t st) {
   if (!s) return e;
   e = rows_alloc(*s, L.N, L.A);
   if (e != cudaSuccess) return e;
-  e = launch_rows_begin(L.v, *s, L.N, L.A, st);
+  e = launch_rows_begin(L.v, *s, L.N, L.A, st, true);
   if (e != cudaSuccess) return e;
   const RowCache& r = *s->rows;
   e = cudaMemsetAsync(L.deg, 0, (size_t)L.A * 4, st);
@@ -1163,7 +1163,7 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   } else {
     e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return (int32_t)e;
-    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture);
+    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true);
     for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = learned_tick(*L, *s, k, features_on, L->capture);
     if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
     cudaGraph_t g = nullptr;

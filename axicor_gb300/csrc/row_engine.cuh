@@ -203,7 +203,8 @@ __device__ __forceinline__ unsigned long long slot_mix(uint32_t t, uint32_t r) {
 __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__ targets,
                                                     const int16_t* __restrict__ weights, uint32_t N,
                                                     uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
-                                                    uint16_t* __restrict__ cnt, ShardCtl* __restrict__ ctl, uint32_t A) {
+                                                    uint16_t* __restrict__ cnt, ShardCtl* __restrict__ ctl, uint32_t A,
+                                                    uint32_t want_sum) {
   __shared__ uint32_t s_t[AXC_MAX_DENDRITES][33];
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_cnt[32];
@@ -227,6 +228,12 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     if (__syncthreads_and(mine)) break;
   }
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // the block's longest row, largest segment and (when asked) targets checksum,
+  // one atomic each per block
+  __shared__ uint32_t s_bc[8], s_bs[8];
+  __shared__ unsigned long long s_bh[8];
+  uint32_t wc = 0, ws = 0;
+  unsigned long long wh = 0;
   for (uint32_t j = warp; j < 32; j += 8) {
     const uint32_t n = n0 + j;
     if (n >= N) continue;
@@ -243,21 +250,31 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
         bad = true;
       }
       smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
-      hsum += slot_mix(t, n * kRowStride + q);
+      if (want_sum) hsum += slot_mix(t, n * kRowStride + q);
       rt[(size_t)n * kRowStride + q] = t;
       rw[(size_t)n * kRowStride + q] = s_w[q][j];
     }
     bad = __any_sync(kFull, bad);
     smx = __reduce_max_sync(kFull, smx);
-    hsum = warp_sum(hsum);
+    if (want_sum) hsum = warp_sum(hsum);
     if (lane == 0) {
       cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
       if (c) {
-        atomicMax(&ctl->row_smax, c);
-        atomicMax(&ctl->seg_max, smx);
-        atomicAdd(&ctl->row_sum, hsum + slot_mix(c, n));
+        wc = max(wc, c);
+        ws = max(ws, smx);
+        wh += hsum + slot_mix(c, n);
       }
     }
+  }
+  if (lane == 0) { s_bc[warp] = wc; s_bs[warp] = ws; s_bh[warp] = wh; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t bc = 0, bs = 0;
+    unsigned long long bh = 0;
+    for (int q = 0; q < 8; q++) { bc = max(bc, s_bc[q]); bs = max(bs, s_bs[q]); bh += s_bh[q]; }
+    if (bc > *(volatile uint32_t*)&ctl->row_smax) atomicMax(&ctl->row_smax, bc);
+    if (bs > *(volatile uint32_t*)&ctl->seg_max) atomicMax(&ctl->seg_max, bs);
+    if (want_sum) atomicAdd(&ctl->row_sum, bh);
   }
 }
 
@@ -893,7 +910,8 @@ void rows_free(ShardScratch& s) {
   s.rows = nullptr;
 }
 
-cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream) {
+cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
+                              bool row_sum) {
   RowCache& r = *s.rows;
   k_rows_reset_lists<<<1, 1, 0, stream>>>(s.ctl);
   cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
@@ -901,7 +919,7 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
   if (N) {
     k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
     k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt,
-                                                    s.ctl, A);
+                                                    s.ctl, A, row_sum ? 1u : 0u);
   }
   return cudaGetLastError();
 }
