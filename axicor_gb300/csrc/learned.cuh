@@ -417,6 +417,7 @@ __global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L,
   __syncthreads();
   const uint32_t count = c.spk_count;
   const uint32_t smax = ctl->row_smax;
+  const RowShape sh = row_shape(smax);
   const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -427,20 +428,11 @@ __global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L,
     const uint32_t n = valid ? spk[idx] : 0u;
     const uint8_t flags = P.soma_flags[n];
     const uint32_t cw = valid ? cnt[n] : 0u;
-    const uint32_t* trow = rt + (size_t)n * kRowStride + 4u * g8;
-    int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
+    const uint32_t* rt_n = rt + (size_t)n * kRowStride;
+    int16_t* rw_n = rw + (size_t)n * kRowStride;
     uint4 T[4];
     uint2 W[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      if (valid && 32u * j + 4u * g8 < smax) {
-        T[j] = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
-        W[j] = *reinterpret_cast<const uint2*>(wrow + 32 * j);
-      } else {
-        T[j] = make_uint4(0, 0, 0, 0);
-        W[j] = make_uint2(0, 0);
-      }
-    }
+    row_load(T, W, rt_n, rw_n, g8, valid, sh, smax);
     const uint32_t cc = cw & 0xFFu;
     const uint32_t var = flags >> 4;
     const VariantParameters& p = lut[var];
@@ -448,10 +440,10 @@ __global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L,
     const bool exact = prop == s_pmax;
     const bool gfast = exact && prop <= 16u;
     uint32_t hitb, slowb;
-    (void)row_slots<false>(T, W, cc, g8, mask2, nullptr, 0u, exact, gfast, prop, P.axon_heads, A, hitb, slowb);
+    (void)row_slots<false>(T, W, cc, g8, sh, mask2, nullptr, 0u, exact, gfast, prop, P.axon_heads, A, hitb, slowb);
     if (valid)
-      gdone += row_gsop(W, hitb, slowb, cc, g8, gtab, var, trow, wrow, P.axon_heads, mask2, A, p, flags, dopamine,
-                        ctl, fix, fix_cap, n);
+      gdone += row_gsop(W, T, hitb, slowb, cc, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                        dopamine, ctl, fix, fix_cap, n);
   }
   block_count(gdone, 0, 0, &ctl->ctr[4]);
 }

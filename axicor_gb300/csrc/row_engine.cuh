@@ -504,19 +504,66 @@ __device__ __forceinline__ void build_gtab(int2 (*gtab)[16], const VariantParame
   }
 }
 
-// The dendrite pass over the 16 slots one lane holds (slots 32j + 4g8 + i of
-// a row with c used slots): returns the lane's share of the input current and
-// sets, per slot (bit 4j+i), hitb = the segment is hit and slowb = GSOP needs
-// the exact path (physics.cu:186-207 for the hit test).
+// How the 8 lanes of a neuron hold its row, from the shard's longest row
+// smax: F full rounds of 32 slots (lane g: slots 32j+4g..32j+4g+3, one vector
+// load each of targets and weights) and, for rows that end inside a round, TR
+// single-slot rounds (lane g: slot 32F+g+8t) kept in the round-3 registers
+// (T[3].x / T[3].y, the two halves of W[3].x).  A 100-slot row takes 3 full
+// rounds and one single-slot round instead of 4 full rounds, three quarters of
+// whose last round would be empty; a tail of more than 16 slots takes a full
+// round.
+struct RowShape {
+  uint32_t F, TR;
+};
+
+__device__ __forceinline__ RowShape row_shape(uint32_t smax) {
+  uint32_t F = smax >> 5, tail = smax & 31u;
+  if (tail > 16u) {
+    F++;
+    tail = 0;
+  }
+  return RowShape{F, (tail + 7u) >> 3};
+}
+
+__device__ __forceinline__ void row_load(uint4 (&T)[4], uint2 (&W)[4], const uint32_t* rt_n, const int16_t* rw_n,
+                                         uint32_t g8, bool valid, RowShape sh, uint32_t smax) {
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    T[j] = make_uint4(0, 0, 0, 0);
+    W[j] = make_uint2(0, 0);
+    if (valid && (uint32_t)j < sh.F && 32u * j + 4u * g8 < smax) {
+      T[j] = __ldg(reinterpret_cast<const uint4*>(rt_n + 32 * j + 4 * g8));
+      W[j] = *reinterpret_cast<const uint2*>(rw_n + 32 * j + 4 * g8);
+    }
+  }
+  if (sh.F < 4u && valid) {
+    const uint32_t q0 = 32u * sh.F + g8;
+    if (sh.TR > 0u && q0 < smax) {
+      T[3].x = __ldg(rt_n + q0);
+      W[3].x = (uint16_t)rw_n[q0];
+    }
+    if (sh.TR > 1u && q0 + 8u < smax) {
+      T[3].y = __ldg(rt_n + q0 + 8);
+      W[3].x |= (uint32_t)(uint16_t)rw_n[q0 + 8] << 16;
+    }
+  }
+}
+
+// The dendrite pass over the slots one lane holds (row_shape) of a row with c
+// used slots: returns the lane's share of the input current and sets, per slot
+// (bit 4j+i; single-slot round t: bit 12+t), hitb = the segment is hit and
+// slowb = GSOP needs the exact path (physics.cu:186-207 for the hit test).
 template <bool LIT>
 __device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&W)[4], uint32_t c, uint32_t g8,
-                                             const uint2* __restrict__ mask2, const uint32_t* s_lit, uint32_t seg_hi,
-                                             bool exact, bool gfast, uint32_t prop, const BurstHeads8* heads,
-                                             uint32_t A, uint32_t& hitb_out, uint32_t& slowb_out) {
+                                             RowShape sh, const uint2* __restrict__ mask2, const uint32_t* s_lit,
+                                             uint32_t seg_hi, bool exact, bool gfast, uint32_t prop,
+                                             const BurstHeads8* heads, uint32_t A, uint32_t& hitb_out,
+                                             uint32_t& slowb_out) {
   int32_t i_in = 0;
   uint32_t hitb = 0, slowb = 0;   // bit 4j+i
 #pragma unroll
   for (int j = 0; j < 4; j++) {
+    if ((uint32_t)j >= sh.F) continue;
     const uint32_t q0 = 32u * j + 4u * g8;
     uint2 m[4];
     bool lit[4];
@@ -549,6 +596,35 @@ __device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&
       // fast GSOP: hit decides, and one same-tick push could not change it
       const bool fast = gfast && s < 31u && !(m[i].y >> 31) && (bx || by == (s == 0u));
       slowb |= fast ? 0u : (1u << (4 * j + i));
+    }
+  }
+  if (sh.F < 4u) {
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      if ((uint32_t)t >= sh.TR) continue;
+      const uint32_t q = 32u * sh.F + g8 + 8u * t;
+      if (q >= c) continue;
+      const uint32_t tw = t ? T[3].y : T[3].x;
+      const uint32_t ax = (tw & AXC_TARGET_AXON_MASK) - 1u;
+      const uint32_t b = 1u << (12 + t);
+      const int32_t w = (int32_t)half_of(W[3], t);
+      if (LIT && gfast && ((tw >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u)) {
+        i_in = wadd(i_in, w);
+        hitb |= b;
+        continue;
+      }
+      const uint2 m = __ldg(mask2 + ax);
+      const uint32_t s = tw >> AXC_TARGET_SEG_SHIFT;
+      const uint32_t shv = min(s, 31u);
+      const uint32_t bx = (m.x >> shv) & 1u, by = (m.y >> shv) & 1u;
+      bool hit = (bx | by) != 0u;
+      if (hit && (s >= 31u || !exact)) hit = hit_exact(heads, A, ax, s, prop);
+      if (hit) {
+        i_in = wadd(i_in, w);
+        hitb |= b;
+      }
+      const bool fast = gfast && s < 31u && !(m.y >> 31) && (bx || by == (s == 0u));
+      slowb |= fast ? 0u : b;
     }
   }
   hitb_out = hitb;
@@ -595,16 +671,18 @@ __device__ __forceinline__ GlifOut glif_step(const VariantParameters& p, int32_t
 
 // GSOP of a spiker's slots held by this lane (physics.cu:281-373): fast slots
 // from the gtab deltas, slow ones on the exact path or deferred to the fix-up
-// list.  Writes the changed weights back to the row; returns the slots done.
-__device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint32_t slowb, uint32_t c, uint32_t g8,
-                                             const int2 (*gtab)[16], uint32_t var, const uint32_t* trow,
-                                             int16_t* wrow, const BurstHeads8* heads, const uint2* mask2,
-                                             uint32_t A, const VariantParameters& p, uint8_t flags,
-                                             int32_t dopamine, ShardCtl* ctl, uint32_t* fix, uint32_t fix_cap,
-                                             uint32_t n) {
+// list.  Writes the changed weights back to the row (rt_n / rw_n: the
+// neuron's row); returns the slots done.
+__device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], const uint4 (&T)[4], uint32_t hitb, uint32_t slowb,
+                                             uint32_t c, uint32_t g8, RowShape sh, const int2 (*gtab)[16],
+                                             uint32_t var, const uint32_t* rt_n, int16_t* rw_n,
+                                             const BurstHeads8* heads, const uint2* mask2, uint32_t A,
+                                             const VariantParameters& p, uint8_t flags, int32_t dopamine,
+                                             ShardCtl* ctl, uint32_t* fix, uint32_t fix_cap, uint32_t n) {
   uint32_t gdone = 0;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
+    if ((uint32_t)j >= sh.F) continue;
     const uint32_t q0 = 32u * j + 4u * g8;
     if (q0 >= c) continue;
     uint2 wj = W[j];
@@ -623,7 +701,7 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
         gdone++;
         continue;
       }
-      const uint32_t t = __ldg(trow + 32 * j + i);
+      const uint32_t t = __ldg(rt_n + q0 + i);
       int16_t nw = w16;
       const int r = gsop_general(heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u, t >> AXC_TARGET_SEG_SHIFT, p,
                                  flags, dopamine, &nw);
@@ -637,7 +715,39 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
       }
       set_half(wj, i, nw);
     }
-    if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(wrow + 32 * j) = wj;
+    if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(rw_n + q0) = wj;
+  }
+  if (sh.F < 4u) {
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+      if ((uint32_t)t >= sh.TR) continue;
+      const uint32_t q = 32u * sh.F + g8 + 8u * t;
+      if (q >= c) continue;
+      const uint32_t b = 1u << (12 + t);
+      const int16_t w16 = half_of(W[3], t);
+      int16_t nw = w16;
+      if (!(slowb & b)) {
+        const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+        const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
+        int32_t na = aw + ((hitb & b) ? e.x : -e.y);
+        na = min(max(na, 0), 32767);
+        nw = (int16_t)(w16 < 0 ? -na : na);
+        gdone++;
+      } else {
+        const uint32_t tw = t ? T[3].y : T[3].x;
+        const int r = gsop_general(heads, mask2, A, (tw & AXC_TARGET_AXON_MASK) - 1u, tw >> AXC_TARGET_SEG_SHIFT,
+                                   p, flags, dopamine, &nw);
+        if (r == 2) continue;
+        gdone++;
+        if (r == 1) {
+          const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+          if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q);
+          else ctl->fix_overflow = 1u;
+          continue;
+        }
+      }
+      if (nw != w16) rw_n[q] = nw;
+    }
   }
   return gdone;
 }
@@ -670,6 +780,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   __syncthreads();
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t smax = ctl->row_smax;   // longest row of the shard: rows are loaded up to here
+  const RowShape sh = row_shape(smax);
   const uint32_t seg_hi = min(ctl->seg_max, 30u);   // lit bits cover segments 1..seg_hi
   const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -688,20 +799,11 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       const uint32_t cw = valid ? cnt[n] : 0u;
       const int32_t thr0 = P.threshold_offset[n];
       const int32_t v0 = P.soma_voltage[n];
-      const uint32_t* trow = rt + (size_t)n * kRowStride + 4u * g8;
-      int16_t* wrow = rw + (size_t)n * kRowStride + 4u * g8;
+      const uint32_t* rt_n = rt + (size_t)n * kRowStride;
+      int16_t* rw_n = rw + (size_t)n * kRowStride;
       uint4 T[4];
       uint2 W[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        if (valid && 32u * j + 4u * g8 < smax) {
-          T[j] = __ldg(reinterpret_cast<const uint4*>(trow + 32 * j));
-          W[j] = *reinterpret_cast<const uint2*>(wrow + 32 * j);
-        } else {
-          T[j] = make_uint4(0, 0, 0, 0);
-          W[j] = make_uint2(0, 0);
-        }
-      }
+      row_load(T, W, rt_n, rw_n, g8, valid, sh, smax);
       const uint32_t c = cw & 0xFFu;
       const uint32_t var = flags >> 4;
       const VariantParameters& p = lut[var];
@@ -710,8 +812,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       const bool gfast = exact && prop <= 16u;
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
       uint32_t hitb, slowb;
-      int32_t i_in = row_slots<LIT>(T, W, c, g8, mask2, s_lit, seg_hi, exact, gfast, prop, P.axon_heads, A, hitb,
-                                    slowb);
+      int32_t i_in = row_slots<LIT>(T, W, c, g8, sh, mask2, s_lit, seg_hi, exact, gfast, prop, P.axon_heads, A,
+                                    hitb, slowb);
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
@@ -739,8 +841,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       }
       // GSOP on the row in registers (physics.cu:281-373)
       if (spike)
-        gdone += row_gsop(W, hitb, slowb, c, g8, gtab, var, trow, wrow, P.axon_heads, mask2, A, p, flags, dopamine,
-                          ctl, fix, fix_cap, n);
+        gdone += row_gsop(W, T, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                          dopamine, ctl, fix, fix_cap, n);
     }
   }
   const uint32_t err_any = __reduce_or_sync(kFull, err);
