@@ -158,3 +158,37 @@ def test_engines_interleave_on_one_shard(gpu):
             assert np.array_equal(vram.download_state(), h_state), (mode, use_graph)
     finally:
         lib.axc_batch_engine_mode(prev)
+
+
+@pytest.mark.parametrize("slots", [12, 40, 100, 110, 120])
+def test_row_shapes(gpu, slots):
+    """Rows that end inside a 32-slot round (single-slot tail rounds) and rows
+    whose tail takes a full round."""
+    w = W.small(dims=(16, 16, 8), slots=slots, inputs=64, p=0.1)
+    lay, state, heads = stress_brain(w, seed=9)
+    spikes, ctr = run_batches(w, lay, state, heads, nb=2, batch=16)
+    assert spikes > 0 and ctr[4] > 0
+
+
+@pytest.mark.parametrize("curve", ["rank0_only", "four_ranks"])
+def test_frozen_weight_groups(gpu, curve):
+    """Weights in ranks whose GSOP deltas are zero cannot move; the update
+    pass skips such slot groups.  Weights are planted on both sides of the
+    rank boundary, at +-32767 and at -32768 (which the clamp moves)."""
+    w = W.small(dims=(16, 16, 8), slots=100, inputs=64, p=0.1)
+    if curve == "four_ranks":
+        for v in (0, 1):
+            w.lut[v]["inertia_curve"] = np.array([128, 96, 64, 32] + [0] * 12, np.uint8)
+    lay, state, heads = S.generate_brain(w.spec())
+    sv = StateView(state, lay.padded_n)
+    rng = np.random.default_rng(4)
+    live = sv.targets != 0
+    edge = 2048 if curve == "rank0_only" else 8192
+    pool = np.array([edge - 1, edge, edge + 1, edge + 300, 20000, 32767, 100, 700], np.int32)
+    mag = rng.choice(pool, size=sv.weights.shape)
+    sign = np.where(sv.weights < 0, -1, 1)
+    neww = (sign * mag).astype(np.int16)
+    neww[(rng.random(sv.weights.shape) < 0.01) & (sign < 0)] = -32768
+    sv.weights[live] = neww[live]
+    spikes, ctr = run_batches(w, lay, state, heads, nb=3, batch=16)
+    assert spikes > 0 and ctr[4] > 0
