@@ -408,15 +408,12 @@ __global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L,
   if (c.mode != 1u || c.overflow) return;
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
-  __shared__ int32_t s_fz[16];
   __shared__ uint32_t s_pmax;
   lut_to_smem(lut);
   if (threadIdx.x == 0) s_pmax = lut_pmax();
   __syncthreads();
   const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
   build_gtab(gtab, lut, dopamine);
-  __syncthreads();
-  build_frozen(s_fz, gtab);
   __syncthreads();
   const uint32_t count = c.spk_count;
   const uint32_t smax = ctl->row_smax;
@@ -445,8 +442,8 @@ __global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L,
     uint32_t hitb, slowb;
     (void)row_slots<false>(T, W, cc, g8, sh, mask2, nullptr, 0u, exact, gfast, prop, P.axon_heads, A, hitb, slowb);
     if (valid)
-      gdone += row_gsop(W, T, hitb, slowb, cc, g8, sh, gtab, s_fz[var], var, rt_n, rw_n, P.axon_heads, mask2, A, p,
-                        flags, dopamine, ctl, fix, fix_cap, n);
+      gdone += row_gsop(W, T, hitb, slowb, cc, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                        dopamine, ctl, fix, fix_cap, n);
   }
   block_count(gdone, 0, 0, &ctl->ctr[4]);
 }

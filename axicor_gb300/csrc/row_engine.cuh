@@ -504,30 +504,6 @@ __device__ __forceinline__ void build_gtab(int2 (*gtab)[16], const VariantParame
   }
 }
 
-// Per variant, the smallest |w| from which every inertia rank has zero GSOP
-// deltas (0x10000: none): such weights cannot move, whatever the hit (except
-// -32768, which the clamp turns into -32767).  Called by the first 16
-// threads after gtab is complete.
-__device__ __forceinline__ void build_frozen(int32_t* fz, const int2 (*gtab)[16]) {
-  if (threadIdx.x < 16) {
-    int r0 = 16;
-    while (r0 > 0 && gtab[threadIdx.x][r0 - 1].x == 0 && gtab[threadIdx.x][r0 - 1].y == 0) r0--;
-    fz[threadIdx.x] = r0 < 16 ? max(r0 * 2048, 1) : 0x10000;
-  }
-}
-
-// True when all four weights of a slot group satisfy thr <= |w| <= 32767.
-__device__ __forceinline__ bool frozen4(uint2 w, int32_t thr) {
-  const int32_t v[4] = {(int16_t)(w.x & 0xFFFFu), (int32_t)w.x >> 16, (int16_t)(w.y & 0xFFFFu), (int32_t)w.y >> 16};
-  bool ok = true;
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int32_t a = abs(v[i]);
-    ok = ok && a >= thr && a <= 32767;
-  }
-  return ok;
-}
-
 // How the 8 lanes of a neuron hold its row, from the shard's longest row
 // smax: F full rounds of 32 slots (lane g: slots 32j+4g..32j+4g+3, one vector
 // load each of targets and weights) and, for rows that end inside a round, TR
@@ -699,7 +675,7 @@ __device__ __forceinline__ GlifOut glif_step(const VariantParameters& p, int32_t
 // neuron's row); returns the slots done.
 __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], const uint4 (&T)[4], uint32_t hitb, uint32_t slowb,
                                              uint32_t c, uint32_t g8, RowShape sh, const int2 (*gtab)[16],
-                                             int32_t fz, uint32_t var, const uint32_t* rt_n, int16_t* rw_n,
+                                             uint32_t var, const uint32_t* rt_n, int16_t* rw_n,
                                              const BurstHeads8* heads, const uint2* mask2, uint32_t A,
                                              const VariantParameters& p, uint8_t flags, int32_t dopamine,
                                              ShardCtl* ctl, uint32_t* fix, uint32_t fix_cap, uint32_t n) {
@@ -710,11 +686,6 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], const uint4 (&T)[4],
     const uint32_t q0 = 32u * j + 4u * g8;
     if (q0 >= c) continue;
     uint2 wj = W[j];
-    // four fast slots whose weights sit in zero-delta ranks stay as they are
-    if (!((slowb >> (4 * j)) & 0xFu) && frozen4(wj, fz)) {
-      gdone += min(c - q0, 4u);
-      continue;
-    }
 #pragma unroll
     for (int i = 0; i < 4; i++) {
       const uint32_t b = 1u << (4 * j + i);
@@ -793,7 +764,6 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   const LearnCtl* __restrict__ lc) {
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];   // GSOP (potentiation, depression) per variant and inertia rank
-  __shared__ int32_t s_fz[16];
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
@@ -807,8 +777,6 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   const uint32_t tick = ctl->tick_base + k;
   const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
   build_gtab(gtab, lut, dopamine);
-  __syncthreads();
-  build_frozen(s_fz, gtab);
   __syncthreads();
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t smax = ctl->row_smax;   // longest row of the shard: rows are loaded up to here
@@ -873,8 +841,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       }
       // GSOP on the row in registers (physics.cu:281-373)
       if (spike)
-        gdone += row_gsop(W, T, hitb, slowb, c, g8, sh, gtab, s_fz[var], var, rt_n, rw_n, P.axon_heads, mask2, A, p,
-                          flags, dopamine, ctl, fix, fix_cap, n);
+        gdone += row_gsop(W, T, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                          dopamine, ctl, fix, fix_cap, n);
     }
   }
   const uint32_t err_any = __reduce_or_sync(kFull, err);
