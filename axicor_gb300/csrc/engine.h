@@ -33,7 +33,6 @@ struct RowCache {
   uint16_t* cnt = nullptr;  // [N] slots before the first empty target; bit 15: an invalid target
   uint2* mask2 = nullptr;   // [A+1] split segment-hit masks (heads 0..6 | head 7); [A] dummy
   uint32_t* mult = nullptr; // [A] number of somas that own the axon
-  uint32_t* owner = nullptr; // [A] the owning soma when mult == 1
   uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
   uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each

@@ -279,8 +279,7 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
 }
 
 __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ s2a, uint32_t N, uint32_t A,
-                                                   uint32_t* __restrict__ mult, uint32_t* __restrict__ owner,
-                                                   uint2* __restrict__ mask2,
+                                                   uint32_t* __restrict__ mult, uint2* __restrict__ mask2,
                                                    ShardCtl* __restrict__ ctl) {
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n == 0) {
@@ -291,10 +290,7 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
   }
   if (n >= N) return;
   const uint32_t a = s2a[n];
-  if (a < A) {
-    atomicAdd(&mult[a], 1u);
-    owner[a] = n;   // meaningful when the axon has one owner
-  }
+  if (a < A) atomicAdd(&mult[a], 1u);
 }
 
 // batch end: weights rows -> columnar for slots before the first empty target.
@@ -372,7 +368,6 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint32_t nv, uint32_t* __restrict__ incoming,
                                                        const uint32_t* __restrict__ batch_counts, uint32_t k,
                                                        uint2* __restrict__ mask2, const uint32_t* __restrict__ mult,
-                                                       const uint32_t* __restrict__ owner,
                                                        uint8_t* __restrict__ flags, uint8_t* __restrict__ timers,
                                                        uint32_t N, uint32_t* __restrict__ eval,
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err,
@@ -415,21 +410,12 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
       if (h[j] != AXC_AXON_SENTINEL) h[j] += v_seg;
     p[0] = make_uint4(h[0], h[1], h[2], h[3]);
     p[1] = make_uint4(h[4], h[5], h[6], h[7]);
-    const uint32_t mu = mult[i];
-    const uint2 m = split_masks(h, s_pmax, mu);
+    const uint2 m = split_masks(h, s_pmax, mult[i]);
     mask2[i] = m;
-    // fully lit: every segment 1..seg_max the batch uses is hit, at most one
-    // soma owns the axon, and no push of this tick can change the hit or the
-    // GSOP outcome there — because heads 0..6 alone cover them, or because the
-    // owner is refractory this tick (a timer > 0 before this tick's countdown;
-    // a countdown already applied can only make the test fail, never pass)
-    bool quiet = false;
-    if (mu == 1u) {
-      const uint32_t o = owner[i];
-      quiet = o < N && *reinterpret_cast<const volatile uint8_t*>(timers + o) > 0;
-    }
-    lit = !(m.y >> 31) &&
-          ((m.x & s_need) == s_need || (quiet && ((m.x | m.y) & s_need) == s_need));
+    // fully lit: heads 0..6 hit every segment 1..seg_max the batch uses and at
+    // most one soma owns the axon, so for those segments the hit is 1 and one
+    // push cannot change it
+    lit = (m.x & s_need) == s_need && !(m.y >> 31);
     if (LEARN) {
       // active: some head covers a segment that a slot of the batch uses
       if (((m.x | (m.y & 0x7FFFFFFFu)) & s_act) != 0u) fan = __ldg(L.inv_off + i + 1) - __ldg(L.inv_off + i);
@@ -892,8 +878,7 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
                                                     const uint2* __restrict__ mask2, const uint32_t* __restrict__ pend,
                                                     const uint32_t* __restrict__ eval,
                                                     const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
-                                                    uint32_t k, const uint32_t* __restrict__ lit_bits,
-                                                    uint32_t lit_used, const LearnCtl* __restrict__ lc) {
+                                                    uint32_t k) {
   const uint32_t nfix = ctl->fix_count;
   const uint32_t overflow = ctl->fix_overflow;
   if (nfix == 0 && !overflow) return;
@@ -910,9 +895,6 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
     return;
   }
   // the list overflowed: rescan every spiker's slots with the update pass's rule
-  // (fully-lit slots were applied on the spot when the LIT update ran this tick)
-  const bool lit_on = lit_used && !(lc && lc->mode == 1u && !lc->overflow);
-  const uint32_t seg_hi = min(ctl->seg_max, 30u);
   const uint32_t ecount = ctl->eval_count[k & 1];
   for (uint32_t w = tid; w < ecount * kRowStride; w += stride) {
     const uint32_t n = eval[w / kRowStride], q = w % kRowStride;
@@ -925,7 +907,6 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
     const VariantParameters& p = lut[P.soma_flags[n] >> 4];
     const uint32_t prop = p.signal_propagation_length;
     const bool gfast = prop == s_pmax && prop <= 16u;
-    if (lit_on && gfast && (s - 1u) < seg_hi && ((lit_bits[a >> 5] >> (a & 31u)) & 1u)) continue;
     const uint2 m = mask2[a];
     const uint32_t sh = min(s, 31u);
     const uint32_t bx = (m.x >> sh) & 1u, by = (m.y >> sh) & 1u;
@@ -999,7 +980,6 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_cnt = off; off = al(off + (size_t)N * 2);
   const size_t o_m2 = off; off = al(off + ((size_t)A + 1) * 8);
   const size_t o_mult = off; off = al(off + (size_t)A * 4);
-  const size_t o_owner = off; off = al(off + (size_t)A * 4);
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
@@ -1018,7 +998,6 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->cnt = reinterpret_cast<uint16_t*>(b + o_cnt);
   r->mask2 = reinterpret_cast<uint2*>(b + o_m2);
   r->mult = reinterpret_cast<uint32_t*>(b + o_mult);
-  r->owner = reinterpret_cast<uint32_t*>(b + o_owner);
   r->eval = reinterpret_cast<uint32_t*>(b + o_eval);
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
@@ -1040,7 +1019,7 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
   cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
   if (e != cudaSuccess) return e;
   if (N) {
-    k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.owner, r.mask2, s.ctl);
+    k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
     k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt,
                                                     s.ctl, A, row_sum ? 1u : 0u);
   }
@@ -1078,13 +1057,11 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   if (G)
     k_rows_prologue<false><<<(G + 255) / 256, 256, 0, stream>>>(
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
-        have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, r.owner, v.soma_flags, v.timers, N, r.eval,
-        s.ctl,
+        have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
         raise, r.lit, LearnDev{});
   if (ev) cudaEventRecord(ev[2], stream);
   const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
-  const bool lit_used = lit_bytes <= lit_smem_limit();
-  if (lit_used) {
+  if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                         s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit, nullptr);
   } else {
@@ -1092,8 +1069,7 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
                                                       s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit, nullptr);
   }
   if (ev) cudaEventRecord(ev[3], stream);
-  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
-                                            r.lit, lit_used ? 1u : 0u, nullptr);
+  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, r.eval, v.soma_flags, N,
                                            a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0, s.ctl,
