@@ -182,6 +182,7 @@ extern "C" int32_t axc_step_day_phase_batch(const ShardVramPtrs* vram, uint32_t 
         a.batch = true;
         a.k = k;
         a.rows = rows != 0;
+        a.defer_push = rows != 0 && k + 1 < sync_batch_ticks;
         a.fix_cap = key.fix_cap;
         le = launch_tick(*vram, *s, a, gc->capture);
       }
@@ -253,6 +254,7 @@ extern "C" int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_
     a.batch = rows;
     a.k = k;
     a.rows = rows;
+    a.defer_push = rows && k + 1 < ticks;
     a.fix_cap = g_fix_cap.load();
     e = launch_tick(*vram, *s, a, st, ev);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[kTickStages]);

@@ -91,6 +91,8 @@ struct TickArgs {
   uint32_t k;                 // tick index inside the batch
   bool rows;                  // use the neuron-major row engine (batch mode only)
   uint32_t fix_cap;           // row engine: deferred-GSOP list capacity (<= kFixCap)
+  bool defer_push;            // row engine: leave this tick's soma pushes to the next tick's prologue
+                              // (never on the last tick of a batch)
 };
 
 // ev (optional): 6 events recorded around the stages (incoming, axons,

@@ -957,9 +957,10 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool fe
     k_rows_prologue<true><<<(G + 255) / 256, 256, 0, st>>>(L.v.axon_heads, A, L.v_seg, bits_k, L.voff,
                                                            bits_k ? L.nv : 0u, s.incoming, nullptr, k, r.mask2,
                                                            r.mult, L.v.soma_flags, L.v.timers, N, r.eval, s.ctl,
-                                                           raise, r.lit, D);
+                                                           raise, r.lit, D, nullptr);
   learned_update_forms(L, s, k, st);
-  k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k);
+  k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k,
+                                        nullptr, nullptr, 0);
   k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
                                        nullptr, nullptr, 0, s.ctl, k);
   if (features_on && L.T)

@@ -371,7 +371,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint8_t* __restrict__ flags, uint8_t* __restrict__ timers,
                                                        uint32_t N, uint32_t* __restrict__ eval,
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err,
-                                                       uint32_t* __restrict__ lit_bits, LearnDev L) {
+                                                       uint32_t* __restrict__ lit_bits, LearnDev L,
+                                                       uint32_t* __restrict__ pend_apply) {
   __shared__ uint32_t s_pmax, s_base, s_need, s_act;
   __shared__ int s_inc;
   __shared__ uint32_t s_warp[8];
@@ -385,6 +386,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
     if (blockIdx.x == 0) {
       ctl->ctr[0] += 1;
       if (raise_err) atomicOr(&ctl->err, raise_err);
+      ctl->fix_count = 0;      // the previous tick's fix-up is done
+      ctl->fix_overflow = 0;
     }
   }
   __syncthreads();
@@ -403,6 +406,10 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
     if (s_inc) {
       const uint32_t c = incoming[i];
       if (c) { npush += c; incoming[i] = 0; }
+    }
+    if (pend_apply) {   // the previous tick's soma pushes (pushes commute: each inserts a zero head)
+      const uint32_t c = pend_apply[i];
+      if (c) { npush += c; pend_apply[i] = 0; }
     }
     push_n(h, npush);
 #pragma unroll
@@ -878,9 +885,27 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
                                                     const uint2* __restrict__ mask2, const uint32_t* __restrict__ pend,
                                                     const uint32_t* __restrict__ eval,
                                                     const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
-                                                    uint32_t k) {
+                                                    uint32_t k, const uint32_t* __restrict__ ids,
+                                                    uint8_t* __restrict__ out, uint32_t num_outputs) {
   const uint32_t nfix = ctl->fix_count;
   const uint32_t overflow = ctl->fix_overflow;
+  {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0) ctl->eval_count[(k + 1) & 1] = 0;   // the next tick's list (last used two ticks ago)
+    // readout of the tick (physics.cu:378-395): flags are final once the update pass is done
+    uint32_t err = 0;
+    for (uint32_t j = tid; j < num_outputs; j += stride) {
+      const uint32_t id = ids[j];
+      uint8_t v = 0;
+      if (id != AXC_NO_AXON) {
+        if (id < N) v = P.soma_flags[id] & 0x01;
+        else err = AXC_ERR_READOUT_RANGE;
+      }
+      out[j] = v;
+    }
+    if (err) atomicOr(&ctl->err, err);
+  }
   if (nfix == 0 && !overflow) return;
   __shared__ VariantParameters lut[16];
   __shared__ uint32_t s_pmax;
@@ -1058,7 +1083,7 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
     k_rows_prologue<false><<<(G + 255) / 256, 256, 0, stream>>>(
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
-        raise, r.lit, LearnDev{});
+        raise, r.lit, LearnDev{}, a.k > 0 ? s.pend : nullptr);
   if (ev) cudaEventRecord(ev[2], stream);
   const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
   if (lit_bytes <= lit_smem_limit()) {
@@ -1069,11 +1094,13 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
                                                       s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit, nullptr);
   }
   if (ev) cudaEventRecord(ev[3], stream);
-  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
-  k_rows_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, r.eval, v.soma_flags, N,
-                                           a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0, s.ctl,
-                                           a.k);
+  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
+                                            a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0);
+  // the soma pushes: by the next tick's prologue within a batch, here on its last tick
+  if (!a.defer_push)
+    k_rows_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, r.eval, v.soma_flags, N,
+                                             nullptr, nullptr, 0, s.ctl, a.k);
   if (ev) {
     cudaEventRecord(ev[4], stream);
     cudaEventRecord(ev[5], stream);
