@@ -37,6 +37,7 @@ namespace {
 constexpr uint32_t kRowStride = AXC_MAX_DENDRITES;   // slots per neuron row
 constexpr uint32_t kInf = 0xFFFFFFFFu;
 constexpr uint32_t kRowBad = 0x8000u;    // cnt flag: the row holds an invalid target
+constexpr uint32_t kRowFrozen = 0x4000u; // cnt flag: no weight of the row can move under GSOP
 
 // physics.cu:322-371 for one slot given the minimum in-tail distance md.
 __device__ __forceinline__ int16_t gsop_weight(int16_t w16, uint32_t md, const VariantParameters& p, int32_t bm,
@@ -200,8 +201,19 @@ __device__ __forceinline__ unsigned long long slot_mix(uint32_t t, uint32_t r) {
 // 32 neurons per 256-thread block; rows are read 8 at a time until every
 // neuron of the tile has met its first empty target.
 // ---------------------------------------------------------------------------
+// Smallest |w| from which every inertia rank of variant v is 0 (0x10000:
+// none): GSOP moves such a weight by 0 whatever the hit, distance, burst or
+// dopamine (physics.cu:336-371), except -32768, which the clamp turns into
+// -32767.
+__device__ __forceinline__ int32_t frozen_from(const VariantParameters& p) {
+  int r0 = 16;
+  while (r0 > 0 && p.inertia_curve[r0 - 1] == 0) r0--;
+  return r0 < 16 ? r0 * 2048 : 0x10000;
+}
+
 __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__ targets,
                                                     const int16_t* __restrict__ weights, uint32_t N,
+                                                    const uint8_t* __restrict__ flags,
                                                     uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
                                                     uint16_t* __restrict__ cnt, ShardCtl* __restrict__ ctl, uint32_t A,
                                                     uint32_t want_sum) {
@@ -238,11 +250,14 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     const uint32_t n = n0 + j;
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
-    bool bad = false;
+    bool bad = false, moves = false;
     uint32_t smx = 0;
     unsigned long long hsum = 0;
+    const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
     for (uint32_t q = lane; q < c; q += 32) {
       uint32_t t = s_t[q][j];
+      const int32_t aw = abs((int32_t)s_w[q][j]);
+      moves = moves || aw < fz || aw > 32767;
       // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
       // which sends the slot down the exact path (hit_exact / gsop_general skip it)
       if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
@@ -255,10 +270,11 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
       rw[(size_t)n * kRowStride + q] = s_w[q][j];
     }
     bad = __any_sync(kFull, bad);
+    moves = __any_sync(kFull, moves);
     smx = __reduce_max_sync(kFull, smx);
     if (want_sum) hsum = warp_sum(hsum);
     if (lane == 0) {
-      cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
+      cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u) | (moves ? 0u : kRowFrozen));
       if (c) {
         wc = max(wc, c);
         ws = max(ws, smx);
@@ -846,8 +862,10 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
           }
         }
       }
-      // GSOP on the row in registers (physics.cu:281-373)
-      if (spike)
+      // GSOP on the row in registers (physics.cu:281-373); a frozen row stays as it is
+      if (spike && (cw & (kRowFrozen | kRowBad)) == kRowFrozen) {
+        if (g8 == 0) gdone += c;
+      } else if (spike)
         gdone += row_gsop(W, T, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
                           dopamine, ctl, fix, fix_cap, n);
     }
@@ -1045,7 +1063,8 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
   if (e != cudaSuccess) return e;
   if (N) {
     k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
-    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt,
+    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, v.soma_flags, r.rt,
+                                                    r.rw, r.cnt,
                                                     s.ctl, A, row_sum ? 1u : 0u);
   }
   return cudaGetLastError();
