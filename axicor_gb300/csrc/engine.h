@@ -20,6 +20,8 @@ struct ShardCtl {
   uint32_t row_smax;      // row engine: longest row (slots before the first empty) of the batch
   uint32_t seg_max;       // row engine: largest segment of a live slot in the batch
   unsigned long long row_sum;  // row engine: checksum of the batch's targets (slot order)
+  uint32_t gsop_count;    // row engine: spikers listed for the GSOP pass of the tick
+  uint32_t pad2;
   unsigned long long ctr[8];  // statistics, see axc_shard_counters
 };
 
@@ -36,6 +38,9 @@ struct RowCache {
   uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
   uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each
+  uint32_t* gs_n = nullptr; // [N] spikers whose rows GSOP may change
+  uint32_t* gs_m = nullptr; // [N][8] their per-lane hit (bits 0..15) and exact-path (bits 16..31) slot masks
+  uint32_t* wcnt = nullptr; // [kMaxUpdateWarps] spikers each warp of the update pass listed
 };
 
 // Per-shard scratch owned by the engine, next to the reference-visible
@@ -57,6 +62,7 @@ struct ShardScratch {
 };
 
 constexpr uint32_t kFixCap = 1u << 22;  // deferred GSOP slots per tick before the rescan path
+constexpr uint32_t kMaxUpdateWarps = 32u * 1024u;  // warps of the update pass (32 per SM)
 
 // Row engine (row_engine.cuh, compiled in day_phase.cu).
 cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix = true);

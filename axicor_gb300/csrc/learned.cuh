@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L,
     if (valid && (cw & (kRowFrozen | kRowBad)) == kRowFrozen) {
       if (g8 == 0) gdone += cc;   // no weight of the row can move
     } else if (valid)
-      gdone += row_gsop(W, T, hitb, slowb, cc, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+      gdone += row_gsop(W, hitb, slowb, cc, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
                         dopamine, ctl, fix, fix_cap, n);
   }
   block_count(gdone, 0, 0, &ctl->ctr[4]);
@@ -931,13 +931,7 @@ static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, cudaSt
   const int sms = sm_count();
   const LearnDev D = L.dev();
   const uint32_t fix_cap = kFixCap;
-  const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
-  if (lit_bytes <= lit_smem_limit())
-    k_rows_update<true><<<sms, 1024, lit_bytes, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                     s.ctl, k, fix_cap, r.lit, L.ctl);
-  else
-    k_rows_update<false><<<4 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                   s.ctl, k, fix_cap, r.lit, L.ctl);
+  launch_rows_update(L.v, s, N, A, k, fix_cap, L.ctl, st);
   k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw,
                                                                 L.v.soma_flags, L.v.axon_heads, A, L.acc, s.ctl);
   k_learn_update<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, L.spk, s.ctl, k);

@@ -696,7 +696,7 @@ __device__ __forceinline__ GlifOut glif_step(const VariantParameters& p, int32_t
 // from the gtab deltas, slow ones on the exact path or deferred to the fix-up
 // list.  Writes the changed weights back to the row (rt_n / rw_n: the
 // neuron's row); returns the slots done.
-__device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], const uint4 (&T)[4], uint32_t hitb, uint32_t slowb,
+__device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint32_t slowb,
                                              uint32_t c, uint32_t g8, RowShape sh, const int2 (*gtab)[16],
                                              uint32_t var, const uint32_t* rt_n, int16_t* rw_n,
                                              const BurstHeads8* heads, const uint2* mask2, uint32_t A,
@@ -757,7 +757,7 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], const uint4 (&T)[4],
         nw = (int16_t)(w16 < 0 ? -na : na);
         gdone++;
       } else {
-        const uint32_t tw = t ? T[3].y : T[3].x;
+        const uint32_t tw = __ldg(rt_n + q);
         const int r = gsop_general(heads, mask2, A, (tw & AXC_TARGET_AXON_MASK) - 1u, tw >> AXC_TARGET_SEG_SHIFT,
                                    p, flags, dopamine, &nw);
         if (r == 2) continue;
@@ -784,9 +784,9 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
                   const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
                   ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits,
-                  const LearnCtl* __restrict__ lc) {
+                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint32_t* __restrict__ gs_m,
+                  uint32_t* __restrict__ wcnt) {
   __shared__ VariantParameters lut[16];
-  __shared__ int2 gtab[16][16];   // GSOP (potentiation, depression) per variant and inertia rank
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
@@ -798,9 +798,6 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   }
   __syncthreads();
   const uint32_t tick = ctl->tick_base + k;
-  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
-  build_gtab(gtab, lut, dopamine);
-  __syncthreads();
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t smax = ctl->row_smax;   // longest row of the shard: rows are loaded up to here
   const RowShape sh = row_shape(smax);
@@ -812,6 +809,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   const uint32_t per_warp = (((ecount + nwarps - 1) / nwarps) + 3) & ~3u;
   const uint32_t beg = min(wid * per_warp, ecount), end = min(beg + per_warp, ecount);
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
+  uint32_t wc = 0;   // spikers this warp listed for the GSOP pass
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t mine = (base + lane < end) ? __ldg(eval + base + lane) : 0u;
     for (uint32_t sub = 0; sub < 32 && base + sub < end; sub += 4) {
@@ -862,18 +860,76 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
           }
         }
       }
-      // GSOP on the row in registers (physics.cu:281-373); a frozen row stays as it is
-      if (spike && (cw & (kRowFrozen | kRowBad)) == kRowFrozen) {
-        if (g8 == 0) gdone += c;
-      } else if (spike)
-        gdone += row_gsop(W, T, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
-                          dopamine, ctl, fix, fix_cap, n);
+      // GSOP (physics.cu:281-373) runs in k_rows_gsop over the spikers listed
+      // here with their slot masks, in this warp's segment of the list; a
+      // frozen row cannot change and is only counted
+      const bool listed = spike && (cw & (kRowFrozen | kRowBad)) != kRowFrozen;
+      if (spike && !listed && g8 == 0) gdone += c;
+      const uint32_t lb = __ballot_sync(kFull, listed && g8 == 0);
+      if (listed) {
+        const uint32_t idx = beg + wc + __popc(lb & ((1u << (lane & ~7u)) - 1u));
+        gs_m[(size_t)idx * 8 + g8] = (hitb & 0xFFFFu) | (slowb << 16);
+        if (g8 == 0) gs_n[idx] = n;
+      }
+      wc += __popc(lb);
     }
   }
+  if (lane == 0) wcnt[wid] = wc;
   const uint32_t err_any = __reduce_or_sync(kFull, err);
   if (err_any && lane == 0) atomicOr(&ctl->err, err_any);
   block_count(ev_slots, hits, nspk, &ctl->ctr[1]);
   block_count(gdone, nev, 0, &ctl->ctr[4]);
+}
+
+// ---------------------------------------------------------------------------
+// per tick 2b: GSOP of the listed spikers (physics.cu:281-373), 8 lanes per
+// row as in the update pass.  Warp w of the update pass listed its spikers at
+// [beg_w, beg_w + wcnt[w]) of the list, beg_w being its slice of the
+// evaluated list.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
+                                                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
+                                                   const uint2* __restrict__ mask2, const uint32_t* __restrict__ gs_n,
+                                                   const uint32_t* __restrict__ gs_m, const uint32_t* __restrict__ wcnt,
+                                                   uint32_t nwu, uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
+                                                   uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
+  if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
+  __shared__ VariantParameters lut[16];
+  __shared__ int2 gtab[16][16];
+  lut_to_smem(lut);
+  __syncthreads();
+  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
+  build_gtab(gtab, lut, dopamine);
+  __syncthreads();
+  const uint32_t ecount = ctl->eval_count[k & 1];
+  const uint32_t per_warp = (((ecount + nwu - 1) / nwu) + 3) & ~3u;
+  const uint32_t smax = ctl->row_smax;
+  const RowShape sh = row_shape(smax);
+  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
+  const uint32_t ngw = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long gdone = 0;
+  for (uint32_t uw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; uw < nwu; uw += ngw) {
+    const uint32_t cntw = wcnt[uw];
+    const uint32_t beg = min(uw * per_warp, ecount);
+    for (uint32_t e = 0; e < cntw; e += 4) {
+      const bool valid = e + grp < cntw;
+      const uint32_t idx = beg + e + grp;
+      const uint32_t n = valid ? gs_n[idx] : 0u;
+      const uint32_t m = valid ? gs_m[(size_t)idx * 8 + g8] : 0u;
+      const uint8_t flags = P.soma_flags[n];
+      const uint32_t c = valid ? (cnt[n] & 0xFFu) : 0u;
+      const uint32_t var = flags >> 4;
+      const uint32_t* rt_n = rt + (size_t)n * kRowStride;
+      int16_t* rw_n = rw + (size_t)n * kRowStride;
+      uint4 T[4];
+      uint2 W[4];
+      row_load(T, W, rt_n, rw_n, g8, valid, sh, smax);
+      if (valid)
+        gdone += row_gsop(W, m & 0xFFFFu, m >> 16, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A,
+                          lut[var], flags, dopamine, ctl, fix, fix_cap, n);
+    }
+  }
+  block_count(gdone, 0, 0, &ctl->ctr[4]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1026,6 +1082,9 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
+  const size_t o_gsn = off; off = al(off + (size_t)N * 4 + 4);
+  const size_t o_gsm = off; off = al(off + (size_t)N * 32 + 32);
+  const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 4);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
   if (e != cudaSuccess) return e;
@@ -1044,6 +1103,9 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->eval = reinterpret_cast<uint32_t*>(b + o_eval);
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
+  r->gs_n = reinterpret_cast<uint32_t*>(b + o_gsn);
+  r->gs_m = reinterpret_cast<uint32_t*>(b + o_gsm);
+  r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
   s.rows = r;
   return cudaSuccess;
 }
@@ -1089,6 +1151,28 @@ static size_t lit_smem_limit() {
   return limit;
 }
 
+// The update pass (with the fully-lit bitmap in shared memory when it fits)
+// and the GSOP pass over the spikers it listed.  lc: the learned engine's
+// control block (both return at once on its sparse ticks), or null.
+static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, uint32_t k,
+                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream) {
+  RowCache& r = *s.rows;
+  const int sms = sm_count();
+  const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
+  uint32_t nwu;
+  if (lit_bytes <= lit_smem_limit()) {
+    nwu = (uint32_t)sms * 32u;
+    k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_m, r.wcnt);
+  } else {
+    nwu = (uint32_t)sms * 32u;
+    k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_m, r.wcnt);
+  }
+  k_rows_gsop<<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.gs_n, r.gs_m, r.wcnt, nwu, r.fix,
+                                           s.ctl, k, fix_cap, lc);
+}
+
 cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
                              cudaEvent_t* ev, bool have_incoming) {
   RowCache& r = *s.rows;
@@ -1104,14 +1188,7 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
         raise, r.lit, LearnDev{}, a.k > 0 ? s.pend : nullptr);
   if (ev) cudaEventRecord(ev[2], stream);
-  const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
-  if (lit_bytes <= lit_smem_limit()) {
-    k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                        s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit, nullptr);
-  } else {
-    k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                      s.ctl, a.k, min(a.fix_cap, kFixCap), r.lit, nullptr);
-  }
+  launch_rows_update(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream);
   if (ev) cudaEventRecord(ev[3], stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
