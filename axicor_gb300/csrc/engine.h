@@ -39,7 +39,6 @@ struct RowCache {
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
   uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each
   uint32_t* gs_n = nullptr; // [N] spikers whose rows GSOP may change
-  uint32_t* gs_m = nullptr; // [N][8] their per-lane hit (bits 0..15) and exact-path (bits 16..31) slot masks
   uint32_t* wcnt = nullptr; // [kMaxUpdateWarps] spikers each warp of the update pass listed
 };
 

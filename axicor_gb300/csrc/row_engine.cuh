@@ -784,8 +784,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
                   const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
                   ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits,
-                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint32_t* __restrict__ gs_m,
-                  uint32_t* __restrict__ wcnt) {
+                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint32_t* __restrict__ wcnt) {
   __shared__ VariantParameters lut[16];
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
@@ -861,16 +860,12 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
         }
       }
       // GSOP (physics.cu:281-373) runs in k_rows_gsop over the spikers listed
-      // here with their slot masks, in this warp's segment of the list; a
-      // frozen row cannot change and is only counted
+      // here, in this warp's segment of the list; a frozen row cannot change
+      // and is only counted
       const bool listed = spike && (cw & (kRowFrozen | kRowBad)) != kRowFrozen;
       if (spike && !listed && g8 == 0) gdone += c;
       const uint32_t lb = __ballot_sync(kFull, listed && g8 == 0);
-      if (listed) {
-        const uint32_t idx = beg + wc + __popc(lb & ((1u << (lane & ~7u)) - 1u));
-        gs_m[(size_t)idx * 8 + g8] = (hitb & 0xFFFFu) | (slowb << 16);
-        if (g8 == 0) gs_n[idx] = n;
-      }
+      if (listed && g8 == 0) gs_n[beg + wc + __popc(lb & ((1u << lane) - 1u))] = n;
       wc += __popc(lb);
     }
   }
@@ -883,20 +878,24 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
 
 // ---------------------------------------------------------------------------
 // per tick 2b: GSOP of the listed spikers (physics.cu:281-373), 8 lanes per
-// row as in the update pass.  Warp w of the update pass listed its spikers at
-// [beg_w, beg_w + wcnt[w]) of the list, beg_w being its slice of the
-// evaluated list.
+// row as in the update pass, whose slot classification (hit, exact path) is
+// recomputed here from the same masks and fully-lit bits.  Warp w of the update
+// pass listed its spikers at [beg_w, beg_w + wcnt[w]), beg_w being its slice
+// of the evaluated list.
 // ---------------------------------------------------------------------------
+template <bool LIT>
 __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
                                                    int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
-                                                   const uint2* __restrict__ mask2, const uint32_t* __restrict__ gs_n,
-                                                   const uint32_t* __restrict__ gs_m, const uint32_t* __restrict__ wcnt,
+                                                   const uint2* __restrict__ mask2, const uint32_t* __restrict__ lit_bits,
+                                                   const uint32_t* __restrict__ gs_n, const uint32_t* __restrict__ wcnt,
                                                    uint32_t nwu, uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
                                                    uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
+  __shared__ uint32_t s_pmax;
   lut_to_smem(lut);
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
   __syncthreads();
   const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
   build_gtab(gtab, lut, dopamine);
@@ -905,6 +904,7 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
   const uint32_t per_warp = (((ecount + nwu - 1) / nwu) + 3) & ~3u;
   const uint32_t smax = ctl->row_smax;
   const RowShape sh = row_shape(smax);
+  const uint32_t seg_hi = min(ctl->seg_max, 30u);
   const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
   const uint32_t ngw = (gridDim.x * blockDim.x) >> 5;
   unsigned long long gdone = 0;
@@ -913,20 +913,25 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
     const uint32_t beg = min(uw * per_warp, ecount);
     for (uint32_t e = 0; e < cntw; e += 4) {
       const bool valid = e + grp < cntw;
-      const uint32_t idx = beg + e + grp;
-      const uint32_t n = valid ? gs_n[idx] : 0u;
-      const uint32_t m = valid ? gs_m[(size_t)idx * 8 + g8] : 0u;
+      const uint32_t n = valid ? gs_n[beg + e + grp] : 0u;
       const uint8_t flags = P.soma_flags[n];
       const uint32_t c = valid ? (cnt[n] & 0xFFu) : 0u;
       const uint32_t var = flags >> 4;
+      const VariantParameters& p = lut[var];
+      const uint32_t prop = p.signal_propagation_length;
+      const bool exact = prop == s_pmax;
+      const bool gfast = exact && prop <= 16u;
       const uint32_t* rt_n = rt + (size_t)n * kRowStride;
       int16_t* rw_n = rw + (size_t)n * kRowStride;
       uint4 T[4];
       uint2 W[4];
       row_load(T, W, rt_n, rw_n, g8, valid, sh, smax);
+      uint32_t hitb, slowb;
+      (void)row_slots<LIT>(T, W, c, g8, sh, mask2, lit_bits, seg_hi, exact, gfast, prop, P.axon_heads, A, hitb,
+                           slowb);
       if (valid)
-        gdone += row_gsop(W, m & 0xFFFFu, m >> 16, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A,
-                          lut[var], flags, dopamine, ctl, fix, fix_cap, n);
+        gdone += row_gsop(W, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                          dopamine, ctl, fix, fix_cap, n);
     }
   }
   block_count(gdone, 0, 0, &ctl->ctr[4]);
@@ -1083,7 +1088,6 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
   const size_t o_gsn = off; off = al(off + (size_t)N * 4 + 4);
-  const size_t o_gsm = off; off = al(off + (size_t)N * 32 + 32);
   const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 4);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
@@ -1104,7 +1108,6 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
   r->gs_n = reinterpret_cast<uint32_t*>(b + o_gsn);
-  r->gs_m = reinterpret_cast<uint32_t*>(b + o_gsm);
   r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
   s.rows = r;
   return cudaSuccess;
@@ -1159,18 +1162,18 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   RowCache& r = *s.rows;
   const int sms = sm_count();
   const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
-  uint32_t nwu;
+  const uint32_t nwu = (uint32_t)sms * 32u;   // both variants: 32 warps per SM
   if (lit_bytes <= lit_smem_limit()) {
-    nwu = (uint32_t)sms * 32u;
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_m, r.wcnt);
+                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.wcnt);
+    k_rows_gsop<true><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+                                                   r.fix, s.ctl, k, fix_cap, lc);
   } else {
-    nwu = (uint32_t)sms * 32u;
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_m, r.wcnt);
+                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.wcnt);
+    k_rows_gsop<false><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+                                                    r.fix, s.ctl, k, fix_cap, lc);
   }
-  k_rows_gsop<<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.gs_n, r.gs_m, r.wcnt, nwu, r.fix,
-                                           s.ctl, k, fix_cap, lc);
 }
 
 cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
