@@ -441,9 +441,7 @@ __global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L,
     const bool gfast = exact && prop <= 16u;
     uint32_t hitb, slowb;
     (void)row_slots<false>(T, W, cc, g8, sh, mask2, nullptr, 0u, exact, gfast, prop, P.axon_heads, A, hitb, slowb);
-    if (valid && (cw & (kRowFrozen | kRowBad)) == kRowFrozen) {
-      if (g8 == 0) gdone += cc;   // no weight of the row can move
-    } else if (valid)
+    if (valid)
       gdone += row_gsop(W, hitb, slowb, cc, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
                         dopamine, ctl, fix, fix_cap, n);
   }

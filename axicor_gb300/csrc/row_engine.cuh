@@ -37,7 +37,6 @@ namespace {
 constexpr uint32_t kRowStride = AXC_MAX_DENDRITES;   // slots per neuron row
 constexpr uint32_t kInf = 0xFFFFFFFFu;
 constexpr uint32_t kRowBad = 0x8000u;    // cnt flag: the row holds an invalid target
-constexpr uint32_t kRowFrozen = 0x4000u; // cnt flag: no weight of the row can move under GSOP
 
 // physics.cu:322-371 for one slot given the minimum in-tail distance md.
 __device__ __forceinline__ int16_t gsop_weight(int16_t w16, uint32_t md, const VariantParameters& p, int32_t bm,
@@ -213,7 +212,6 @@ __device__ __forceinline__ int32_t frozen_from(const VariantParameters& p) {
 
 __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__ targets,
                                                     const int16_t* __restrict__ weights, uint32_t N,
-                                                    const uint8_t* __restrict__ flags,
                                                     uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
                                                     uint16_t* __restrict__ cnt, ShardCtl* __restrict__ ctl, uint32_t A,
                                                     uint32_t want_sum) {
@@ -250,14 +248,11 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     const uint32_t n = n0 + j;
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
-    bool bad = false, moves = false;
+    bool bad = false;
     uint32_t smx = 0;
     unsigned long long hsum = 0;
-    const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
     for (uint32_t q = lane; q < c; q += 32) {
       uint32_t t = s_t[q][j];
-      const int32_t aw = abs((int32_t)s_w[q][j]);
-      moves = moves || aw < fz || aw > 32767;
       // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
       // which sends the slot down the exact path (hit_exact / gsop_general skip it)
       if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
@@ -270,11 +265,10 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
       rw[(size_t)n * kRowStride + q] = s_w[q][j];
     }
     bad = __any_sync(kFull, bad);
-    moves = __any_sync(kFull, moves);
     smx = __reduce_max_sync(kFull, smx);
     if (want_sum) hsum = warp_sum(hsum);
     if (lane == 0) {
-      cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u) | (moves ? 0u : kRowFrozen));
+      cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
       if (c) {
         wc = max(wc, c);
         ws = max(ws, smx);
@@ -572,6 +566,64 @@ __device__ __forceinline__ void row_load(uint4 (&T)[4], uint2 (&W)[4], const uin
   }
 }
 
+// Live slots (before c) that lane g8 holds.
+__device__ __forceinline__ uint32_t lane_live(uint32_t c, uint32_t g8, RowShape sh) {
+  uint32_t k = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t q0 = 32u * j + 4u * g8;
+    if ((uint32_t)j < sh.F && q0 < c) k += min(c - q0, 4u);
+  }
+  if (sh.F < 4u) {
+#pragma unroll
+    for (int t = 0; t < 2; t++)
+      if ((uint32_t)t < sh.TR && 32u * sh.F + g8 + 8u * t < c) k++;
+  }
+  return k;
+}
+
+// batch start, after the row copy: bit g of lfz[n] says that every live slot
+// lane g holds of neuron n's row (row_shape) has a weight GSOP cannot move
+// (frozen_from).  Weights only freeze, so the bit holds for the whole batch.
+// Rows with an invalid target keep every lane live.
+__global__ void __launch_bounds__(256) k_rows_lanes(const int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
+                                                    const uint8_t* __restrict__ flags, uint32_t N,
+                                                    const ShardCtl* __restrict__ ctl, uint8_t* __restrict__ lfz) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t n = t >> 3, g8 = t & 7u;
+  const RowShape sh = row_shape(ctl->row_smax);
+  bool frozen = false;
+  if (n < N) {
+    const uint32_t cw = cnt[n], c = cw & 0xFFu;
+    if (!(cw & kRowBad)) {
+      const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
+      const int16_t* rw_n = rw + (size_t)n * kRowStride;
+      frozen = true;
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint32_t q = 32u * j + 4u * g8 + i;
+          if ((uint32_t)j < sh.F && q < c) {
+            const int32_t aw = abs((int32_t)rw_n[q]);
+            frozen = frozen && aw >= fz && aw <= 32767;
+          }
+        }
+      if (sh.F < 4u)
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+          const uint32_t q = 32u * sh.F + g8 + 8u * u;
+          if ((uint32_t)u < sh.TR && q < c) {
+            const int32_t aw = abs((int32_t)rw_n[q]);
+            frozen = frozen && aw >= fz && aw <= 32767;
+          }
+        }
+    }
+  }
+  const uint32_t b = __ballot_sync(kFull, frozen);
+  if (g8 == 0 && n < N) lfz[n] = (uint8_t)((b >> (threadIdx.x & 24u)) & 0xFFu);
+}
+
 // The dendrite pass over the slots one lane holds (row_shape) of a row with c
 // used slots: returns the lane's share of the input current and sets, per slot
 // (bit 4j+i; single-slot round t: bit 12+t), hitb = the segment is hit and
@@ -784,7 +836,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
                   const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
                   ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits,
-                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint32_t* __restrict__ wcnt) {
+                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint8_t* __restrict__ gs_l,
+                  const uint8_t* __restrict__ lfz, uint32_t* __restrict__ wcnt) {
   __shared__ VariantParameters lut[16];
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
@@ -817,6 +870,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       // every load of the neuron at once: state, count, and its row up to smax
       const uint8_t flags = P.soma_flags[n];
       const uint32_t cw = valid ? cnt[n] : 0u;
+      const uint32_t lf = lfz[n];
       const int32_t thr0 = P.threshold_offset[n];
       const int32_t v0 = P.soma_voltage[n];
       const uint32_t* rt_n = rt + (size_t)n * kRowStride;
@@ -860,12 +914,16 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
         }
       }
       // GSOP (physics.cu:281-373) runs in k_rows_gsop over the spikers listed
-      // here, in this warp's segment of the list; a frozen row cannot change
-      // and is only counted
-      const bool listed = spike && (cw & (kRowFrozen | kRowBad)) != kRowFrozen;
-      if (spike && !listed && g8 == 0) gdone += c;
-      const uint32_t lb = __ballot_sync(kFull, listed && g8 == 0);
-      if (listed && g8 == 0) gs_n[beg + wc + __popc(lb & ((1u << lane) - 1u))] = n;
+      // here with the lanes it may change, in this warp's segment of the list;
+      // frozen lanes are only counted
+      const uint32_t act = spike ? (~lf & 0xFFu) : 0u;   // lanes GSOP may change
+      if (spike && ((lf >> g8) & 1u)) gdone += lane_live(c, g8, sh);
+      const uint32_t lb = __ballot_sync(kFull, act != 0u && g8 == 0);
+      if (act && g8 == 0) {
+        const uint32_t idx = beg + wc + __popc(lb & ((1u << lane) - 1u));
+        gs_n[idx] = n;
+        gs_l[idx] = (uint8_t)act;
+      }
       wc += __popc(lb);
     }
   }
@@ -887,7 +945,8 @@ template <bool LIT>
 __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
                                                    int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
                                                    const uint2* __restrict__ mask2, const uint32_t* __restrict__ lit_bits,
-                                                   const uint32_t* __restrict__ gs_n, const uint32_t* __restrict__ wcnt,
+                                                   const uint32_t* __restrict__ gs_n, const uint8_t* __restrict__ gs_l,
+                                                   const uint32_t* __restrict__ wcnt,
                                                    uint32_t nwu, uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
                                                    uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
@@ -912,8 +971,9 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
     const uint32_t cntw = wcnt[uw];
     const uint32_t beg = min(uw * per_warp, ecount);
     for (uint32_t e = 0; e < cntw; e += 4) {
-      const bool valid = e + grp < cntw;
-      const uint32_t n = valid ? gs_n[beg + e + grp] : 0u;
+      const bool listed = e + grp < cntw;
+      const uint32_t n = listed ? gs_n[beg + e + grp] : 0u;
+      const bool valid = listed && ((gs_l[beg + e + grp] >> g8) & 1u);   // this lane's slots may change
       const uint8_t flags = P.soma_flags[n];
       const uint32_t c = valid ? (cnt[n] & 0xFFu) : 0u;
       const uint32_t var = flags >> 4;
@@ -1088,6 +1148,8 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
   const size_t o_gsn = off; off = al(off + (size_t)N * 4 + 4);
+  const size_t o_gsl = off; off = al(off + (size_t)N + 4);
+  const size_t o_lfz = off; off = al(off + (size_t)N + 4);
   const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 4);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
@@ -1108,6 +1170,8 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
   r->gs_n = reinterpret_cast<uint32_t*>(b + o_gsn);
+  r->gs_l = reinterpret_cast<uint8_t*>(b + o_gsl);
+  r->lfz = reinterpret_cast<uint8_t*>(b + o_lfz);
   r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
   s.rows = r;
   return cudaSuccess;
@@ -1128,9 +1192,9 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
   if (e != cudaSuccess) return e;
   if (N) {
     k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
-    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, v.soma_flags, r.rt,
-                                                    r.rw, r.cnt,
+    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt,
                                                     s.ctl, A, row_sum ? 1u : 0u);
+    k_rows_lanes<<<(N * 8 + 255) / 256, 256, 0, stream>>>(r.rw, r.cnt, v.soma_flags, N, s.ctl, r.lfz);
   }
   return cudaGetLastError();
 }
@@ -1165,13 +1229,14 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   const uint32_t nwu = (uint32_t)sms * 32u;   // both variants: 32 warps per SM
   if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.wcnt);
-    k_rows_gsop<true><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_l, r.lfz, r.wcnt);
+    k_rows_gsop<true><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.gs_l, r.wcnt, nwu,
                                                    r.fix, s.ctl, k, fix_cap, lc);
   } else {
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.wcnt);
-    k_rows_gsop<false><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_l, r.lfz, r.wcnt);
+    k_rows_gsop<false><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.gs_l, r.wcnt,
+                                                    nwu,
                                                     r.fix, s.ctl, k, fix_cap, lc);
   }
 }
