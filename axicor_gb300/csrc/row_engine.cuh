@@ -582,6 +582,13 @@ __device__ __forceinline__ uint32_t lane_live(uint32_t c, uint32_t g8, RowShape 
   return k;
 }
 
+// thr <= |w| <= 32767, in plain signed comparisons (-32768 is not frozen: the
+// clamp moves it).
+__device__ __forceinline__ bool frozen_weight(int16_t w16, int32_t thr) {
+  const int32_t w = w16;
+  return w != -32768 && (w >= thr || w <= -thr);
+}
+
 // batch start, after the row copy: bit g of lfz[n] says that every live slot
 // lane g holds of neuron n's row (row_shape) has a weight GSOP cannot move
 // (frozen_from).  Weights only freeze, so the bit holds for the whole batch.
@@ -604,19 +611,13 @@ __global__ void __launch_bounds__(256) k_rows_lanes(const int16_t* __restrict__ 
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           const uint32_t q = 32u * j + 4u * g8 + i;
-          if ((uint32_t)j < sh.F && q < c) {
-            const int32_t aw = abs((int32_t)rw_n[q]);
-            frozen = frozen && aw >= fz && aw <= 32767;
-          }
+          if ((uint32_t)j < sh.F && q < c) frozen = frozen && frozen_weight(rw_n[q], fz);
         }
       if (sh.F < 4u)
 #pragma unroll
         for (int u = 0; u < 2; u++) {
           const uint32_t q = 32u * sh.F + g8 + 8u * u;
-          if ((uint32_t)u < sh.TR && q < c) {
-            const int32_t aw = abs((int32_t)rw_n[q]);
-            frozen = frozen && aw >= fz && aw <= 32767;
-          }
+          if ((uint32_t)u < sh.TR && q < c) frozen = frozen && frozen_weight(rw_n[q], fz);
         }
     }
   }
