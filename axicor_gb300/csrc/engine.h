@@ -38,8 +38,7 @@ struct RowCache {
   uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
   uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each
-  uint32_t* gs_n = nullptr; // [N] spikers whose rows GSOP may change
-  uint8_t* gs_l = nullptr;  // [N] their lanes (bit g) GSOP may change
+  uint32_t* gs_n = nullptr; // [8N] (spiker, lane) pairs GSOP may change: 8 n + lane
   uint8_t* lfz = nullptr;   // [N] lanes (bit g) whose slots GSOP cannot move (set at batch start)
   uint32_t* wcnt = nullptr; // [kMaxUpdateWarps] spikers each warp of the update pass listed
 };

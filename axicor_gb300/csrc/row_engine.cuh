@@ -837,8 +837,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
                   const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
                   ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits,
-                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint8_t* __restrict__ gs_l,
-                  const uint8_t* __restrict__ lfz, uint32_t* __restrict__ wcnt) {
+                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, const uint8_t* __restrict__ lfz,
+                  uint32_t* __restrict__ wcnt) {
   __shared__ VariantParameters lut[16];
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
@@ -862,7 +862,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   const uint32_t per_warp = (((ecount + nwarps - 1) / nwarps) + 3) & ~3u;
   const uint32_t beg = min(wid * per_warp, ecount), end = min(beg + per_warp, ecount);
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
-  uint32_t wc = 0;   // spikers this warp listed for the GSOP pass
+  uint32_t wc = 0;   // (spiker, lane) pairs this warp listed for the GSOP pass
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t mine = (base + lane < end) ? __ldg(eval + base + lane) : 0u;
     for (uint32_t sub = 0; sub < 32 && base + sub < end; sub += 4) {
@@ -914,18 +914,14 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
           }
         }
       }
-      // GSOP (physics.cu:281-373) runs in k_rows_gsop over the spikers listed
-      // here with the lanes it may change, in this warp's segment of the list;
-      // frozen lanes are only counted
-      const uint32_t act = spike ? (~lf & 0xFFu) : 0u;   // lanes GSOP may change
-      if (spike && ((lf >> g8) & 1u)) gdone += lane_live(c, g8, sh);
-      const uint32_t lb = __ballot_sync(kFull, act != 0u && g8 == 0);
-      if (act && g8 == 0) {
-        const uint32_t idx = beg + wc + __popc(lb & ((1u << lane) - 1u));
-        gs_n[idx] = n;
-        gs_l[idx] = (uint8_t)act;
-      }
-      wc += __popc(lb);
+      // GSOP (physics.cu:281-373) runs in k_rows_gsop over the (spiker, lane)
+      // pairs listed here, in this warp's segment of the list; frozen lanes
+      // are only counted
+      const bool frozen_lane = (lf >> g8) & 1u;
+      if (spike && frozen_lane) gdone += lane_live(c, g8, sh);
+      const uint32_t ab = __ballot_sync(kFull, spike && !frozen_lane);
+      if (spike && !frozen_lane) gs_n[8u * beg + wc + __popc(ab & ((1u << lane) - 1u))] = n * 8u + g8;
+      wc += __popc(ab);
     }
   }
   if (lane == 0) wcnt[wid] = wc;
@@ -936,18 +932,17 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
 }
 
 // ---------------------------------------------------------------------------
-// per tick 2b: GSOP of the listed spikers (physics.cu:281-373), 8 lanes per
-// row as in the update pass, whose slot classification (hit, exact path) is
-// recomputed here from the same masks and fully-lit bits.  Warp w of the update
-// pass listed its spikers at [beg_w, beg_w + wcnt[w]), beg_w being its slice
-// of the evaluated list.
+// per tick 2b: GSOP (physics.cu:281-373) of the listed (spiker, lane) pairs,
+// one thread per pair: the lane's slots of the row (row_shape), their
+// classification (hit, exact path) recomputed from the tick's masks and
+// fully-lit bits, then row_gsop.  Warp w of the update pass listed its pairs
+// at [8 beg_w, 8 beg_w + wcnt[w]), beg_w being its slice of the evaluated list.
 // ---------------------------------------------------------------------------
 template <bool LIT>
 __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
                                                    int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
                                                    const uint2* __restrict__ mask2, const uint32_t* __restrict__ lit_bits,
-                                                   const uint32_t* __restrict__ gs_n, const uint8_t* __restrict__ gs_l,
-                                                   const uint32_t* __restrict__ wcnt,
+                                                   const uint32_t* __restrict__ gs_n, const uint32_t* __restrict__ wcnt,
                                                    uint32_t nwu, uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
                                                    uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
@@ -965,18 +960,17 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
   const uint32_t smax = ctl->row_smax;
   const RowShape sh = row_shape(smax);
   const uint32_t seg_hi = min(ctl->seg_max, 30u);
-  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
+  const uint32_t lane = threadIdx.x & 31;
   const uint32_t ngw = (gridDim.x * blockDim.x) >> 5;
   unsigned long long gdone = 0;
   for (uint32_t uw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; uw < nwu; uw += ngw) {
     const uint32_t cntw = wcnt[uw];
-    const uint32_t beg = min(uw * per_warp, ecount);
-    for (uint32_t e = 0; e < cntw; e += 4) {
-      const bool listed = e + grp < cntw;
-      const uint32_t n = listed ? gs_n[beg + e + grp] : 0u;
-      const bool valid = listed && ((gs_l[beg + e + grp] >> g8) & 1u);   // this lane's slots may change
+    const size_t base = 8u * (size_t)min(uw * per_warp, ecount);
+    for (uint32_t e = lane; e < cntw; e += 32) {
+      const uint32_t item = gs_n[base + e];
+      const uint32_t n = item >> 3, g8 = item & 7u;
       const uint8_t flags = P.soma_flags[n];
-      const uint32_t c = valid ? (cnt[n] & 0xFFu) : 0u;
+      const uint32_t c = cnt[n] & 0xFFu;
       const uint32_t var = flags >> 4;
       const VariantParameters& p = lut[var];
       const uint32_t prop = p.signal_propagation_length;
@@ -986,13 +980,12 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
       int16_t* rw_n = rw + (size_t)n * kRowStride;
       uint4 T[4];
       uint2 W[4];
-      row_load(T, W, rt_n, rw_n, g8, valid, sh, smax);
+      row_load(T, W, rt_n, rw_n, g8, true, sh, smax);
       uint32_t hitb, slowb;
       (void)row_slots<LIT>(T, W, c, g8, sh, mask2, lit_bits, seg_hi, exact, gfast, prop, P.axon_heads, A, hitb,
                            slowb);
-      if (valid)
-        gdone += row_gsop(W, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
-                          dopamine, ctl, fix, fix_cap, n);
+      gdone += row_gsop(W, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                        dopamine, ctl, fix, fix_cap, n);
     }
   }
   block_count(gdone, 0, 0, &ctl->ctr[4]);
@@ -1148,8 +1141,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
-  const size_t o_gsn = off; off = al(off + (size_t)N * 4 + 4);
-  const size_t o_gsl = off; off = al(off + (size_t)N + 4);
+  const size_t o_gsn = off; off = al(off + (size_t)N * 32 + 4);
   const size_t o_lfz = off; off = al(off + (size_t)N + 4);
   const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 4);
   void* base = nullptr;
@@ -1171,7 +1163,6 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
   r->gs_n = reinterpret_cast<uint32_t*>(b + o_gsn);
-  r->gs_l = reinterpret_cast<uint8_t*>(b + o_gsl);
   r->lfz = reinterpret_cast<uint8_t*>(b + o_lfz);
   r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
   s.rows = r;
@@ -1230,14 +1221,13 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   const uint32_t nwu = (uint32_t)sms * 32u;   // both variants: 32 warps per SM
   if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_l, r.lfz, r.wcnt);
-    k_rows_gsop<true><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.gs_l, r.wcnt, nwu,
+                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
+    k_rows_gsop<true><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
                                                    r.fix, s.ctl, k, fix_cap, lc);
   } else {
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gs_l, r.lfz, r.wcnt);
-    k_rows_gsop<false><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.gs_l, r.wcnt,
-                                                    nwu,
+                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
+    k_rows_gsop<false><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
                                                     r.fix, s.ctl, k, fix_cap, lc);
   }
 }
