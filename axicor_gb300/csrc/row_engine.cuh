@@ -1218,16 +1218,17 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   RowCache& r = *s.rows;
   const int sms = sm_count();
   const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
-  const uint32_t nwu = (uint32_t)sms * 32u;   // both variants: 32 warps per SM
+  const uint32_t nwu = (uint32_t)sms * 32u;   // both variants: 32 warps per SM; the GSOP pass: a warp per
+                                               // update warp's segment
   if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                         s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
-    k_rows_gsop<true><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+    k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
                                                    r.fix, s.ctl, k, fix_cap, lc);
   } else {
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                       s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
-    k_rows_gsop<false><<<2 * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+    k_rows_gsop<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
                                                     r.fix, s.ctl, k, fix_cap, lc);
   }
 }
