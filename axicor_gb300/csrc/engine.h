@@ -38,8 +38,9 @@ struct RowCache {
   uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
   uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each
-  uint32_t* gs_n = nullptr; // [8N] (spiker, lane) pairs GSOP may change: 8 n + lane
-  uint8_t* lfz = nullptr;   // [N] lanes (bit g) whose slots GSOP cannot move (set at batch start)
+  uint32_t* gs_n = nullptr; // [N] spikers with slots GSOP may move
+  uint4* amask = nullptr;   // [N] slots (bit q) whose weights GSOP may move (set at batch start)
+  uint8_t* lfz = nullptr;   // [N] 1: every slot of the row is frozen (set at batch start)
   uint32_t* wcnt = nullptr; // [kMaxUpdateWarps] spikers each warp of the update pass listed
 };
 

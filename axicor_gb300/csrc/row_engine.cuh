@@ -566,22 +566,6 @@ __device__ __forceinline__ void row_load(uint4 (&T)[4], uint2 (&W)[4], const uin
   }
 }
 
-// Live slots (before c) that lane g8 holds.
-__device__ __forceinline__ uint32_t lane_live(uint32_t c, uint32_t g8, RowShape sh) {
-  uint32_t k = 0;
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const uint32_t q0 = 32u * j + 4u * g8;
-    if ((uint32_t)j < sh.F && q0 < c) k += min(c - q0, 4u);
-  }
-  if (sh.F < 4u) {
-#pragma unroll
-    for (int t = 0; t < 2; t++)
-      if ((uint32_t)t < sh.TR && 32u * sh.F + g8 + 8u * t < c) k++;
-  }
-  return k;
-}
-
 // thr <= |w| <= 32767, in plain signed comparisons (-32768 is not frozen: the
 // clamp moves it).
 __device__ __forceinline__ bool frozen_weight(int16_t w16, int32_t thr) {
@@ -589,40 +573,37 @@ __device__ __forceinline__ bool frozen_weight(int16_t w16, int32_t thr) {
   return w != -32768 && (w >= thr || w <= -thr);
 }
 
-// batch start, after the row copy: bit g of lfz[n] says that every live slot
-// lane g holds of neuron n's row (row_shape) has a weight GSOP cannot move
-// (frozen_from).  Weights only freeze, so the bit holds for the whole batch.
-// Rows with an invalid target keep every lane live.
+// batch start, after the row copy: bit q of amask[n] is set when the weight
+// of live slot q may still move under GSOP (not frozen_weight, or the row
+// holds an invalid target); lfz[n] = 1 when no bit is set.  Weights only
+// freeze, so both hold for the whole batch.  A thread per (neuron, 16-slot
+// chunk).
 __global__ void __launch_bounds__(256) k_rows_lanes(const int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
                                                     const uint8_t* __restrict__ flags, uint32_t N,
-                                                    const ShardCtl* __restrict__ ctl, uint8_t* __restrict__ lfz) {
+                                                    uint4* __restrict__ amask, uint8_t* __restrict__ lfz) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t n = t >> 3, g8 = t & 7u;
-  const RowShape sh = row_shape(ctl->row_smax);
-  bool frozen = false;
+  const uint32_t n = t >> 3, part = t & 7u;   // slots 16 part .. 16 part + 15
+  uint32_t bits = 0;
   if (n < N) {
     const uint32_t cw = cnt[n], c = cw & 0xFFu;
-    if (!(cw & kRowBad)) {
-      const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
-      const int16_t* rw_n = rw + (size_t)n * kRowStride;
-      frozen = true;
+    const bool all = (cw & kRowBad) != 0u;
+    const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
+    const int16_t* rw_n = rw + (size_t)n * kRowStride + 16u * part;
 #pragma unroll
-      for (int j = 0; j < 4; j++)
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const uint32_t q = 32u * j + 4u * g8 + i;
-          if ((uint32_t)j < sh.F && q < c) frozen = frozen && frozen_weight(rw_n[q], fz);
-        }
-      if (sh.F < 4u)
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-          const uint32_t q = 32u * sh.F + g8 + 8u * u;
-          if ((uint32_t)u < sh.TR && q < c) frozen = frozen && frozen_weight(rw_n[q], fz);
-        }
+    for (int i = 0; i < 16; i++) {
+      const uint32_t q = 16u * part + i;
+      if (q < c && (all || !frozen_weight(rw_n[i], fz))) bits |= 1u << (q & 31u);
     }
   }
-  const uint32_t b = __ballot_sync(kFull, frozen);
-  if (g8 == 0 && n < N) lfz[n] = (uint8_t)((b >> (threadIdx.x & 24u)) & 0xFFu);
+  // word w of the neuron = the two 16-slot chunks 2w and 2w+1
+  const uint32_t other = __shfl_xor_sync(kFull, bits, 1);
+  const uint32_t word = bits | other;
+  const uint32_t w0 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 0), w1 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 2);
+  const uint32_t w2 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 4), w3 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 6);
+  if (part == 0 && n < N) {
+    amask[n] = make_uint4(w0, w1, w2, w3);
+    lfz[n] = (w0 | w1 | w2 | w3) ? 0u : 1u;
+  }
 }
 
 // The dendrite pass over the slots one lane holds (row_shape) of a row with c
@@ -862,7 +843,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   const uint32_t per_warp = (((ecount + nwarps - 1) / nwarps) + 3) & ~3u;
   const uint32_t beg = min(wid * per_warp, ecount), end = min(beg + per_warp, ecount);
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
-  uint32_t wc = 0;   // (spiker, lane) pairs this warp listed for the GSOP pass
+  uint32_t wc = 0;   // spikers this warp listed for the GSOP pass
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t mine = (base + lane < end) ? __ldg(eval + base + lane) : 0u;
     for (uint32_t sub = 0; sub < 32 && base + sub < end; sub += 4) {
@@ -914,13 +895,13 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
           }
         }
       }
-      // GSOP (physics.cu:281-373) runs in k_rows_gsop over the (spiker, lane)
-      // pairs listed here, in this warp's segment of the list; frozen lanes
-      // are only counted
-      const bool frozen_lane = (lf >> g8) & 1u;
-      if (spike && frozen_lane) gdone += lane_live(c, g8, sh);
-      const uint32_t ab = __ballot_sync(kFull, spike && !frozen_lane);
-      if (spike && !frozen_lane) gs_n[8u * beg + wc + __popc(ab & ((1u << lane) - 1u))] = n * 8u + g8;
+      // GSOP (physics.cu:281-373) runs in k_rows_gsop over the spikers listed
+      // here (those with slots that may move), in this warp's segment of the
+      // list; a fully frozen row is only counted
+      const bool listed = spike && !lf;
+      if (spike && lf && g8 == 0) gdone += c;
+      const uint32_t ab = __ballot_sync(kFull, listed && g8 == 0);
+      if (listed && g8 == 0) gs_n[beg + wc + __popc(ab & ((1u << lane) - 1u))] = n;
       wc += __popc(ab);
     }
   }
@@ -932,19 +913,22 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
 }
 
 // ---------------------------------------------------------------------------
-// per tick 2b: GSOP (physics.cu:281-373) of the listed (spiker, lane) pairs,
-// one thread per pair: the lane's slots of the row (row_shape), their
-// classification (hit, exact path) recomputed from the tick's masks and
-// fully-lit bits, then row_gsop.  Warp w of the update pass listed its pairs
-// at [8 beg_w, 8 beg_w + wcnt[w]), beg_w being its slice of the evaluated list.
+// per tick 2b: GSOP (physics.cu:281-373) of the listed spikers, a thread per
+// spiker, over the slots of amask only (the others are frozen: GSOP leaves
+// them as they are).  Each slot is classified as in the update pass (fully lit,
+// else the tick's hit masks; exact path for segments >= 31, other lengths,
+// several owners, or a hit that one same-tick push could change) and updated
+// from the gtab deltas, on the exact path, or deferred to the fix-up stage.
+// Warp w of the update pass listed its spikers at [beg_w, beg_w + wcnt[w]).
 // ---------------------------------------------------------------------------
 template <bool LIT>
 __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
                                                    int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
                                                    const uint2* __restrict__ mask2, const uint32_t* __restrict__ lit_bits,
-                                                   const uint32_t* __restrict__ gs_n, const uint32_t* __restrict__ wcnt,
-                                                   uint32_t nwu, uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
-                                                   uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
+                                                   const uint4* __restrict__ amask, const uint32_t* __restrict__ gs_n,
+                                                   const uint32_t* __restrict__ wcnt, uint32_t nwu,
+                                                   uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl, uint32_t k,
+                                                   uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
@@ -957,18 +941,15 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
   __syncthreads();
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t per_warp = (((ecount + nwu - 1) / nwu) + 3) & ~3u;
-  const uint32_t smax = ctl->row_smax;
-  const RowShape sh = row_shape(smax);
   const uint32_t seg_hi = min(ctl->seg_max, 30u);
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t ngw = (gridDim.x * blockDim.x) >> 5;
   unsigned long long gdone = 0;
   for (uint32_t uw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; uw < nwu; uw += ngw) {
     const uint32_t cntw = wcnt[uw];
-    const size_t base = 8u * (size_t)min(uw * per_warp, ecount);
+    const uint32_t beg = min(uw * per_warp, ecount);
     for (uint32_t e = lane; e < cntw; e += 32) {
-      const uint32_t item = gs_n[base + e];
-      const uint32_t n = item >> 3, g8 = item & 7u;
+      const uint32_t n = gs_n[beg + e];
       const uint8_t flags = P.soma_flags[n];
       const uint32_t c = cnt[n] & 0xFFu;
       const uint32_t var = flags >> 4;
@@ -976,16 +957,54 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
       const uint32_t prop = p.signal_propagation_length;
       const bool exact = prop == s_pmax;
       const bool gfast = exact && prop <= 16u;
-      const uint32_t* rt_n = rt + (size_t)n * kRowStride;
-      int16_t* rw_n = rw + (size_t)n * kRowStride;
-      uint4 T[4];
-      uint2 W[4];
-      row_load(T, W, rt_n, rw_n, g8, true, sh, smax);
-      uint32_t hitb, slowb;
-      (void)row_slots<LIT>(T, W, c, g8, sh, mask2, lit_bits, seg_hi, exact, gfast, prop, P.axon_heads, A, hitb,
-                           slowb);
-      gdone += row_gsop(W, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
-                        dopamine, ctl, fix, fix_cap, n);
+      const uint4 am = amask[n];
+      const uint32_t words[4] = {am.x, am.y, am.z, am.w};
+      gdone += c - (__popc(am.x) + __popc(am.y) + __popc(am.z) + __popc(am.w));   // frozen slots
+#pragma unroll
+      for (int wq = 0; wq < 4; wq++) {
+        uint32_t rest = words[wq];
+        while (rest) {
+          const uint32_t q = 32u * wq + (__ffs(rest) - 1);
+          rest &= rest - 1u;
+          const size_t r = (size_t)n * kRowStride + q;
+          const uint32_t t = __ldg(rt + r);
+          const int16_t w16 = rw[r];
+          const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;
+          const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+          bool hit, fast;
+          if (LIT && gfast && (s - 1u) < seg_hi && ((__ldg(lit_bits + (ax >> 5)) >> (ax & 31u)) & 1u)) {
+            hit = true;
+            fast = true;
+          } else {
+            const uint2 m = __ldg(mask2 + ax);
+            const uint32_t sh = min(s, 31u);
+            const uint32_t bx = (m.x >> sh) & 1u, by = (m.y >> sh) & 1u;
+            hit = (bx | by) != 0u;
+            if (hit && (s >= 31u || !exact)) hit = hit_exact(P.axon_heads, A, ax, s, prop);
+            fast = gfast && s < 31u && !(m.y >> 31) && (bx || by == (s == 0u));
+          }
+          int16_t nw = w16;
+          if (fast) {
+            const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+            const int2 d = gtab[var][min((uint32_t)aw >> 11, 15u)];
+            int32_t na = aw + (hit ? d.x : -d.y);
+            na = min(max(na, 0), 32767);
+            nw = (int16_t)(w16 < 0 ? -na : na);
+            gdone++;
+          } else {
+            const int res = gsop_general(P.axon_heads, mask2, A, ax, s, p, flags, dopamine, &nw);
+            if (res == 2) continue;
+            gdone++;
+            if (res == 1) {
+              const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+              if (slot < fix_cap) fix[slot] = (uint32_t)r;
+              else ctl->fix_overflow = 1u;
+              continue;
+            }
+          }
+          if (nw != w16) rw[r] = nw;
+        }
+      }
     }
   }
   block_count(gdone, 0, 0, &ctl->ctr[4]);
@@ -1141,7 +1160,8 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
-  const size_t o_gsn = off; off = al(off + (size_t)N * 32 + 4);
+  const size_t o_gsn = off; off = al(off + (size_t)N * 4 + 4);
+  const size_t o_am = off; off = al(off + (size_t)N * 16 + 16);
   const size_t o_lfz = off; off = al(off + (size_t)N + 4);
   const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 4);
   void* base = nullptr;
@@ -1163,6 +1183,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
   r->gs_n = reinterpret_cast<uint32_t*>(b + o_gsn);
+  r->amask = reinterpret_cast<uint4*>(b + o_am);
   r->lfz = reinterpret_cast<uint8_t*>(b + o_lfz);
   r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
   s.rows = r;
@@ -1186,7 +1207,7 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
     k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
     k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt,
                                                     s.ctl, A, row_sum ? 1u : 0u);
-    k_rows_lanes<<<(N * 8 + 255) / 256, 256, 0, stream>>>(r.rw, r.cnt, v.soma_flags, N, s.ctl, r.lfz);
+    k_rows_lanes<<<(N * 8 + 255) / 256, 256, 0, stream>>>(r.rw, r.cnt, v.soma_flags, N, r.amask, r.lfz);
   }
   return cudaGetLastError();
 }
@@ -1223,12 +1244,13 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                         s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
-    k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+    k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt, nwu,
                                                    r.fix, s.ctl, k, fix_cap, lc);
   } else {
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                       s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
-    k_rows_gsop<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gs_n, r.wcnt, nwu,
+    k_rows_gsop<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
+                                                    nwu,
                                                     r.fix, s.ctl, k, fix_cap, lc);
   }
 }
