@@ -38,10 +38,11 @@ struct RowCache {
   uint32_t* eval = nullptr; // [N] non-refractory neurons of the tick
   uint32_t* fix = nullptr;  // [kFixCap] deferred GSOP slots (n*128 + slot)
   uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each
-  uint32_t* gs_n = nullptr; // [N] spikers with slots GSOP may move
+  uint32_t* gs_n = nullptr; // [N] spikers with 1..8 slots GSOP may move (a thread each)
+  uint32_t* gd_n = nullptr; // [N] spikers with more (8 lanes each)
   uint4* amask = nullptr;   // [N] slots (bit q) whose weights GSOP may move (set at batch start)
-  uint8_t* lfz = nullptr;   // [N] 1: every slot of the row is frozen (set at batch start)
-  uint32_t* wcnt = nullptr; // [kMaxUpdateWarps] spikers each warp of the update pass listed
+  uint8_t* lfz = nullptr;   // [N] number of those slots (set at batch start)
+  uint32_t* wcnt = nullptr; // [2][kMaxUpdateWarps] spikers each warp of the update pass listed (gs_n, gd_n)
 };
 
 // Per-shard scratch owned by the engine, next to the reference-visible

@@ -575,7 +575,7 @@ __device__ __forceinline__ bool frozen_weight(int16_t w16, int32_t thr) {
 
 // batch start, after the row copy: bit q of amask[n] is set when the weight
 // of live slot q may still move under GSOP (not frozen_weight, or the row
-// holds an invalid target); lfz[n] = 1 when no bit is set.  Weights only
+// holds an invalid target); lfz[n] = the number of such slots.  Weights only
 // freeze, so both hold for the whole batch.  A thread per (neuron, 16-slot
 // chunk).
 __global__ void __launch_bounds__(256) k_rows_lanes(const int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(256) k_rows_lanes(const int16_t* __restrict__ 
   const uint32_t w2 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 4), w3 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 6);
   if (part == 0 && n < N) {
     amask[n] = make_uint4(w0, w1, w2, w3);
-    lfz[n] = (w0 | w1 | w2 | w3) ? 0u : 1u;
+    lfz[n] = (uint8_t)(__popc(w0) + __popc(w1) + __popc(w2) + __popc(w3));
   }
 }
 
@@ -818,8 +818,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
                   const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
                   ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits,
-                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, const uint8_t* __restrict__ lfz,
-                  uint32_t* __restrict__ wcnt) {
+                  const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint32_t* __restrict__ gd_n,
+                  const uint8_t* __restrict__ lfz, uint32_t* __restrict__ wcnt) {
   __shared__ VariantParameters lut[16];
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
@@ -843,7 +843,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   const uint32_t per_warp = (((ecount + nwarps - 1) / nwarps) + 3) & ~3u;
   const uint32_t beg = min(wid * per_warp, ecount), end = min(beg + per_warp, ecount);
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
-  uint32_t wc = 0;   // spikers this warp listed for the GSOP pass
+  uint32_t wc = 0, wd = 0;   // spikers this warp listed for the GSOP passes
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t mine = (base + lane < end) ? __ldg(eval + base + lane) : 0u;
     for (uint32_t sub = 0; sub < 32 && base + sub < end; sub += 4) {
@@ -895,17 +895,23 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
           }
         }
       }
-      // GSOP (physics.cu:281-373) runs in k_rows_gsop over the spikers listed
-      // here (those with slots that may move), in this warp's segment of the
-      // list; a fully frozen row is only counted
-      const bool listed = spike && !lf;
-      if (spike && lf && g8 == 0) gdone += c;
-      const uint32_t ab = __ballot_sync(kFull, listed && g8 == 0);
-      if (listed && g8 == 0) gs_n[beg + wc + __popc(ab & ((1u << lane) - 1u))] = n;
+      // GSOP (physics.cu:281-373) runs in k_rows_gsop / k_rows_gsop_rows over
+      // the spikers listed here (those with slots that may move: a few, or
+      // many), in this warp's segments of the lists; a fully frozen row is only
+      // counted
+      const bool few = spike && lf > 0u && lf <= 8u, many = spike && lf > 8u;
+      if (spike && lf == 0u && g8 == 0) gdone += c;
+      const uint32_t ab = __ballot_sync(kFull, few && g8 == 0), db = __ballot_sync(kFull, many && g8 == 0);
+      if (few && g8 == 0) gs_n[beg + wc + __popc(ab & ((1u << lane) - 1u))] = n;
+      if (many && g8 == 0) gd_n[beg + wd + __popc(db & ((1u << lane) - 1u))] = n;
       wc += __popc(ab);
+      wd += __popc(db);
     }
   }
-  if (lane == 0) wcnt[wid] = wc;
+  if (lane == 0) {
+    wcnt[wid] = wc;
+    wcnt[kMaxUpdateWarps + wid] = wd;
+  }
   const uint32_t err_any = __reduce_or_sync(kFull, err);
   if (err_any && lane == 0) atomicOr(&ctl->err, err_any);
   block_count(ev_slots, hits, nspk, &ctl->ctr[1]);
@@ -1005,6 +1011,65 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
           if (nw != w16) rw[r] = nw;
         }
       }
+    }
+  }
+  block_count(gdone, 0, 0, &ctl->ctr[4]);
+}
+
+// GSOP of the listed spikers with many slots that may move, 8 lanes per row
+// as in the update pass (row_load / row_slots / row_gsop; frozen slots get a
+// zero delta).  Warp w of the update pass listed them at [beg_w, beg_w + wcnt[w]).
+template <bool LIT>
+__global__ void __launch_bounds__(256) k_rows_gsop_rows(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
+                                                        int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
+                                                        const uint2* __restrict__ mask2,
+                                                        const uint32_t* __restrict__ lit_bits,
+                                                        const uint32_t* __restrict__ gd_n,
+                                                        const uint32_t* __restrict__ wcnt, uint32_t nwu,
+                                                        uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
+                                                        uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
+  if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
+  __shared__ VariantParameters lut[16];
+  __shared__ int2 gtab[16][16];
+  __shared__ uint32_t s_pmax;
+  lut_to_smem(lut);
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
+  __syncthreads();
+  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
+  build_gtab(gtab, lut, dopamine);
+  __syncthreads();
+  const uint32_t ecount = ctl->eval_count[k & 1];
+  const uint32_t per_warp = (((ecount + nwu - 1) / nwu) + 3) & ~3u;
+  const uint32_t smax = ctl->row_smax;
+  const RowShape sh = row_shape(smax);
+  const uint32_t seg_hi = min(ctl->seg_max, 30u);
+  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
+  const uint32_t ngw = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long gdone = 0;
+  for (uint32_t uw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; uw < nwu; uw += ngw) {
+    const uint32_t cntw = wcnt[uw];
+    const uint32_t beg = min(uw * per_warp, ecount);
+    for (uint32_t e = 0; e < cntw; e += 4) {
+      const bool valid = e + grp < cntw;
+      const uint32_t n = valid ? gd_n[beg + e + grp] : 0u;
+      const uint8_t flags = P.soma_flags[n];
+      const uint32_t c = valid ? (cnt[n] & 0xFFu) : 0u;
+      const uint32_t var = flags >> 4;
+      const VariantParameters& p = lut[var];
+      const uint32_t prop = p.signal_propagation_length;
+      const bool exact = prop == s_pmax;
+      const bool gfast = exact && prop <= 16u;
+      const uint32_t* rt_n = rt + (size_t)n * kRowStride;
+      int16_t* rw_n = rw + (size_t)n * kRowStride;
+      uint4 T[4];
+      uint2 W[4];
+      row_load(T, W, rt_n, rw_n, g8, valid, sh, smax);
+      uint32_t hitb, slowb;
+      (void)row_slots<LIT>(T, W, c, g8, sh, mask2, lit_bits, seg_hi, exact, gfast, prop, P.axon_heads, A, hitb,
+                           slowb);
+      if (valid)
+        gdone += row_gsop(W, hitb, slowb, c, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                          dopamine, ctl, fix, fix_cap, n);
     }
   }
   block_count(gdone, 0, 0, &ctl->ctr[4]);
@@ -1161,9 +1226,10 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
   const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
   const size_t o_gsn = off; off = al(off + (size_t)N * 4 + 4);
+  const size_t o_gdn = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_am = off; off = al(off + (size_t)N * 16 + 16);
   const size_t o_lfz = off; off = al(off + (size_t)N + 4);
-  const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 4);
+  const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 8);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
   if (e != cudaSuccess) return e;
@@ -1183,6 +1249,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->fix = with_fix ? reinterpret_cast<uint32_t*>(b + o_fix) : nullptr;
   r->lit = reinterpret_cast<uint32_t*>(b + o_lit);
   r->gs_n = reinterpret_cast<uint32_t*>(b + o_gsn);
+  r->gd_n = reinterpret_cast<uint32_t*>(b + o_gdn);
   r->amask = reinterpret_cast<uint4*>(b + o_am);
   r->lfz = reinterpret_cast<uint8_t*>(b + o_lfz);
   r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
@@ -1243,15 +1310,18 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
                                                // update warp's segment
   if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
-    k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt, nwu,
-                                                   r.fix, s.ctl, k, fix_cap, lc);
+                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt);
+    k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
+                                                   nwu, r.fix, s.ctl, k, fix_cap, lc);
+    k_rows_gsop_rows<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
+                                                        r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap, lc);
   } else {
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.lfz, r.wcnt);
+                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt);
     k_rows_gsop<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
-                                                    nwu,
-                                                    r.fix, s.ctl, k, fix_cap, lc);
+                                                    nwu, r.fix, s.ctl, k, fix_cap, lc);
+    k_rows_gsop_rows<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
+                                                         r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap, lc);
   }
 }
 
