@@ -42,7 +42,8 @@ LEARNED = {"learned-1.5M": False, "learned-homeostatic-1.5M": True}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    # 3 warm-up batches + 97 timed = the 10,000 ticks of the 1.5M configuration
+    ap.add_argument("--steps", type=int, default=97)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="plain-1.5M",
@@ -644,7 +645,11 @@ def main():
             "config": {"workload": args.workload, "neurons": r["neurons"], "synapses": r["synapses"],
                        "ticks_per_step": args.ticks_per_step, "parallelism": "replicas" if dist.world > 1 else "single",
                        "l2": "inputs larger than L2 (1.37 GB .state per brain)", "gsop": True,
-                       "engine": r["engine"]},
+                       "engine": r["engine"],
+                       "timed_ticks": [args.warmup * args.ticks_per_step,
+                                       (args.warmup + args.steps) * args.ticks_per_step],
+                       "e2e_ticks": [(args.warmup + args.steps) * args.ticks_per_step,
+                                     (args.warmup + 2 * args.steps) * args.ticks_per_step]},
             "e2e": {"value": r["e2e_events_per_s"], "unit": "events/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ticks_per_s": r["e2e_ticks_per_s"]},
             "gpu_launches": r["launches"],
