@@ -1302,7 +1302,8 @@ static size_t lit_smem_limit() {
 // and the GSOP pass over the spikers it listed.  lc: the learned engine's
 // control block (both return at once on its sparse ticks), or null.
 static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, uint32_t k,
-                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream) {
+                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream,
+                               cudaEvent_t after_update = nullptr) {
   RowCache& r = *s.rows;
   const int sms = sm_count();
   const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
@@ -1311,6 +1312,7 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   if (lit_bytes <= lit_smem_limit()) {
     k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                         s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt);
+    if (after_update) cudaEventRecord(after_update, stream);
     k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
                                                    nwu, r.fix, s.ctl, k, fix_cap, lc);
     k_rows_gsop_rows<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
@@ -1318,6 +1320,7 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   } else {
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                       s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt);
+    if (after_update) cudaEventRecord(after_update, stream);
     k_rows_gsop<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
                                                     nwu, r.fix, s.ctl, k, fix_cap, lc);
     k_rows_gsop_rows<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
@@ -1340,8 +1343,8 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
         raise, r.lit, LearnDev{}, a.k > 0 ? s.pend : nullptr);
   if (ev) cudaEventRecord(ev[2], stream);
-  launch_rows_update(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream);
-  if (ev) cudaEventRecord(ev[3], stream);
+  // stages: ev[2]..ev[3] the update pass, ev[3]..ev[4] the GSOP passes, fix-up and push
+  launch_rows_update(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream, ev ? ev[3] : nullptr);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
                                             a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0);

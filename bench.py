@@ -137,6 +137,11 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+# DRAM traffic per launch of the dominant kernel from one ncu capture of the same kernel on the same
+# workload in its steady state (profiles/k_rows_update_plain-1.5M.md)
+TRAFFIC = {("plain-1.5M", "k_rows_update"): 336.9e6}
+
+
 def workload(name: str):
     from axicor_gb300 import workloads as W
     return getattr(W, CONFIGS[name])()
@@ -162,12 +167,12 @@ def update_kernel_bytes(ticks, evaluated, spikes, N):
     return 6 * evaluated + ticks * 20 * N + 4 * spikes
 
 
-def rows_update_kernel_bytes(evaluated_slots, gsop_slots, evaluated_neurons, spikes):
-    """Algorithmic bytes of the row engine's update+GSOP kernel: 6 B per evaluated slot (u32 target + i16
-    weight read), 2 B per GSOP slot (weight written), 24 B per evaluated neuron (flags, slot count, list
-    entry, voltage and threshold read; voltage, flags, threshold, timer written), 4 B per spike
-    (soma_to_axon)."""
-    return 6 * evaluated_slots + 2 * gsop_slots + 24 * evaluated_neurons + 4 * spikes
+def rows_update_kernel_bytes(evaluated_slots, evaluated_neurons, spikes):
+    """Algorithmic bytes of the row engine's update pass (k_rows_update): 6 B per evaluated slot (u32 target +
+    i16 weight read), 24 B per evaluated neuron (flags, slot count, list entry, voltage and threshold read;
+    voltage, flags, threshold, timer written), 4 B per spike (soma_to_axon).  The weights GSOP changes are
+    written by the GSOP passes."""
+    return 6 * evaluated_slots + 24 * evaluated_neurons + 4 * spikes
 
 
 def run_gb300(args, dist: Dist) -> dict | None:
@@ -274,16 +279,17 @@ def run_gb300(args, dist: Dist) -> dict | None:
         raise RuntimeError(f"axc_profile_ticks failed: {err}")
     stage_ms = list(out_ms)
     if engine == 1:
-        names = ["network_ids", "prologue", "update_gsop", "fixup_push", "gsop"]
-        kernels = {"prologue": "k_rows_prologue", "update_gsop": "k_rows_update", "fixup_push": "k_rows_fixup+k_push"}
+        names = ["network_ids", "prologue", "update", "gsop_fixup_push", "unused"]
+        kernels = {"prologue": "k_rows_prologue", "update": "k_rows_update",
+                   "gsop_fixup_push": "k_rows_gsop+k_rows_gsop_rows+k_rows_fixup+k_rows_push"}
     else:
         names = ["network_ids", "axons", "update", "push", "gsop"]
         kernels = {"axons": "k_axons", "update": "k_update", "push": "k_push", "gsop": "k_gsop"}
     top = int(np.argmax(stage_ms))
     ev, hits, spk, gs, nev = (int(x) for x in out_cnt)
     A_ = lay.total_axons
-    if names[top] == "update_gsop":
-        kb = rows_update_kernel_bytes(ev, gs, nev, spk)
+    if engine == 1 and names[top] == "update":
+        kb = rows_update_kernel_bytes(ev, nev, spk)
     elif names[top] == "update":
         kb = update_kernel_bytes(prof_ticks, ev, spk, lay.padded_n)
     elif names[top] == "gsop":
@@ -312,7 +318,10 @@ def run_gb300(args, dist: Dist) -> dict | None:
         "launches": K * ((4 * B + 5) if engine == 1 else (4 * B + 2)),
         "roofline": {"bound": "hbm", "kernel": kernels.get(names[top], names[top]),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+                     "traffic": TRAFFIC.get((args.workload, kernels.get(names[top], names[top]))),
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "algorithmic_bytes_per_launch": kb / prof_ticks,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
         "stage_ms_per_tick": {n: m / prof_ticks for n, m in zip(names, stage_ms)},
         "tick_algorithmic_gbs": tick_bytes / (ms / 1e3) / 1e9,
         "per_tick": {"evaluated_slots": int(ctr[1]) / ticks_timed, "hits": int(ctr[2]) / ticks_timed,
