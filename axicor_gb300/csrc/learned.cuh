@@ -12,8 +12,8 @@
 //           per-tile segments sized from the prediction, k_learn_scatter walks
 //           an inverted index (axon -> dendrite slots) and adds the weights of
 //           hit slots into the evaluated neurons' input current, k_learn_update
-//           runs GLIF from that current, and k_learn_gsop applies GSOP to the
-//           spikers' rows with the row engine's own slot code.
+//           runs GLIF from that current and lists the spikers for the row
+//           engine's GSOP passes (the same passes as the dense form).
 //
 // A tile whose actual activity exceeds its pre-sized segment sets the overflow
 // flag in the prologue; the dense kernels then run the tick and the sparse
@@ -338,12 +338,16 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
 }
 
 // per tick 3s: GLIF of every evaluated neuron from the scattered current;
-// spikers push their axon and are listed for GSOP.
+// spikers push their axon and are listed for the row engine's GSOP passes
+// exactly as k_rows_update lists them (the same per-warp slices of the
+// evaluated list, 32 warps per SM).
 __global__ void __launch_bounds__(256) k_learn_update(ShardVramPtrs P, LearnDev L, uint32_t A,
                                                       const uint16_t* __restrict__ cnt,
                                                       const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend,
-                                                      int32_t* __restrict__ acc, uint32_t* __restrict__ spk,
-                                                      ShardCtl* __restrict__ ctl, uint32_t k) {
+                                                      int32_t* __restrict__ acc, const uint8_t* __restrict__ lfz,
+                                                      uint32_t* __restrict__ gs_n, uint32_t* __restrict__ gd_n,
+                                                      uint32_t* __restrict__ wcnt, ShardCtl* __restrict__ ctl,
+                                                      uint32_t k) {
   LearnCtl& c = *L.ctl;
   if (c.mode != 1u || c.overflow) return;
   __shared__ VariantParameters lut[16];
@@ -352,18 +356,22 @@ __global__ void __launch_bounds__(256) k_learn_update(ShardVramPtrs P, LearnDev 
   const uint32_t tick = ctl->tick_base + k;
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t stride = gridDim.x * blockDim.x;
-  unsigned long long ev_slots = 0, nspk = 0, nev = 0;
-  uint32_t err = 0;
-  for (uint32_t b0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b0 < ecount; b0 += stride) {
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t per_warp = (((ecount + nwarps - 1) / nwarps) + 3) & ~3u;
+  const uint32_t beg = min(wid * per_warp, ecount), end = min(beg + per_warp, ecount);
+  unsigned long long ev_slots = 0, nspk = 0, nev = 0, gdone = 0;
+  uint32_t err = 0, wc = 0, wd = 0;
+  for (uint32_t b0 = beg; b0 < end; b0 += 32) {
     const uint32_t i = b0 + lane;
-    const bool valid = i < ecount;
+    const bool valid = i < end;
     bool spike = false;
-    uint32_t n = 0;
+    uint32_t n = 0, lf = 0;
     if (valid) {
       n = eval[i];
       const uint8_t flags = P.soma_flags[n];
       const uint32_t cw = cnt[n];
+      lf = lfz[n];
       const int32_t i_in = acc[n];
       acc[n] = 0;
       const VariantParameters& p = lut[flags >> 4];
@@ -378,6 +386,7 @@ __global__ void __launch_bounds__(256) k_learn_update(ShardVramPtrs P, LearnDev 
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
       if (spike) {
         nspk++;
+        if (lf == 0u) gdone += cw & 0xFFu;   // every weight of the row is frozen
         const uint32_t my_axon = P.soma_to_axon[n];
         if (my_axon != AXC_NO_AXON) {
           if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
@@ -385,67 +394,22 @@ __global__ void __launch_bounds__(256) k_learn_update(ShardVramPtrs P, LearnDev 
         }
       }
     }
-    const uint32_t ball = __ballot_sync(kFull, spike);
-    uint32_t base = 0;
-    if (lane == 0 && ball) base = atomicAdd(&c.spk_count, __popc(ball));
-    base = __shfl_sync(kFull, base, 0);
-    if (spike) spk[base + __popc(ball & ((1u << lane) - 1u))] = n;
+    const bool few = spike && lf > 0u && lf <= 8u, many = spike && lf > 8u;
+    const uint32_t ab = __ballot_sync(kFull, few), db = __ballot_sync(kFull, many);
+    const uint32_t below = (1u << lane) - 1u;
+    if (few) gs_n[beg + wc + __popc(ab & below)] = n;
+    if (many) gd_n[beg + wd + __popc(db & below)] = n;
+    wc += __popc(ab);
+    wd += __popc(db);
+  }
+  if (lane == 0) {
+    wcnt[wid] = wc;
+    wcnt[kMaxUpdateWarps + wid] = wd;
   }
   const uint32_t err_any = __reduce_or_sync(kFull, err);
   if (err_any && lane == 0) atomicOr(&ctl->err, err_any);
   block_count(ev_slots, 0, nspk, &ctl->ctr[1]);
-  block_count(0, nev, 0, &ctl->ctr[4]);
-}
-
-// per tick 3s': GSOP of the sparse tick's spikers, 8 lanes per spiker, with
-// the row engine's slot classification and update (row_slots / row_gsop).
-__global__ void __launch_bounds__(256) k_learn_gsop(ShardVramPtrs P, LearnDev L, uint32_t A,
-                                                    const uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
-                                                    const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
-                                                    const uint32_t* __restrict__ spk, uint32_t* __restrict__ fix,
-                                                    ShardCtl* __restrict__ ctl, uint32_t fix_cap) {
-  LearnCtl& c = *L.ctl;
-  if (c.mode != 1u || c.overflow) return;
-  __shared__ VariantParameters lut[16];
-  __shared__ int2 gtab[16][16];
-  __shared__ uint32_t s_pmax;
-  lut_to_smem(lut);
-  if (threadIdx.x == 0) s_pmax = lut_pmax();
-  __syncthreads();
-  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
-  build_gtab(gtab, lut, dopamine);
-  __syncthreads();
-  const uint32_t count = c.spk_count;
-  const uint32_t smax = ctl->row_smax;
-  const RowShape sh = row_shape(smax);
-  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7, grp = lane >> 3;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  unsigned long long gdone = 0;
-  for (uint32_t base = wid * 4; base < count; base += nwarps * 4) {
-    const uint32_t idx = base + grp;
-    const bool valid = idx < count;
-    const uint32_t n = valid ? spk[idx] : 0u;
-    const uint8_t flags = P.soma_flags[n];
-    const uint32_t cw = valid ? cnt[n] : 0u;
-    const uint32_t* rt_n = rt + (size_t)n * kRowStride;
-    int16_t* rw_n = rw + (size_t)n * kRowStride;
-    uint4 T[4];
-    uint2 W[4];
-    row_load(T, W, rt_n, rw_n, g8, valid, sh, smax);
-    const uint32_t cc = cw & 0xFFu;
-    const uint32_t var = flags >> 4;
-    const VariantParameters& p = lut[var];
-    const uint32_t prop = p.signal_propagation_length;
-    const bool exact = prop == s_pmax;
-    const bool gfast = exact && prop <= 16u;
-    uint32_t hitb, slowb;
-    (void)row_slots<false>(T, W, cc, g8, sh, mask2, nullptr, 0u, exact, gfast, prop, P.axon_heads, A, hitb, slowb);
-    if (valid)
-      gdone += row_gsop(W, hitb, slowb, cc, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
-                        dopamine, ctl, fix, fix_cap, n);
-  }
-  block_count(gdone, 0, 0, &ctl->ctr[4]);
+  block_count(gdone, nev, 0, &ctl->ctr[4]);
 }
 
 // ---------------------------------------------------------------------------
@@ -932,13 +896,15 @@ static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, cudaSt
   launch_rows_update(L.v, s, N, A, k, fix_cap, L.ctl, st);
   k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw,
                                                                 L.v.soma_flags, L.v.axon_heads, A, L.acc, s.ctl);
-  k_learn_update<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, L.spk, s.ctl, k);
-  k_learn_gsop<<<2 * sms, 256, 0, st>>>(L.v, D, A, r.rt, r.rw, r.cnt, r.mask2, L.spk, r.fix, s.ctl, fix_cap);
+  // 4 blocks of 256 per SM: the 32 warps per SM whose slices the GSOP passes read
+  k_learn_update<<<4 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, r.lfz, r.gs_n, r.gd_n, r.wcnt,
+                                          s.ctl, k);
 }
 
 // One tick: schedule, prologue, both update forms (the one not picked returns
 // at once), fix-up, push, features + prediction.
-static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool features_on, cudaStream_t st) {
+static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool last, bool features_on,
+                                cudaStream_t st) {
   RowCache& r = *s.rows;
   const uint32_t N = L.N, A = L.A;
   const int sms = sm_count();
@@ -951,11 +917,13 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool fe
     k_rows_prologue<true><<<(G + 255) / 256, 256, 0, st>>>(L.v.axon_heads, A, L.v_seg, bits_k, L.voff,
                                                            bits_k ? L.nv : 0u, s.incoming, nullptr, k, r.mask2,
                                                            r.mult, L.v.soma_flags, L.v.timers, N, r.eval, s.ctl,
-                                                           raise, r.lit, D, nullptr);
+                                                           raise, r.lit, D, k > 0 ? s.pend : nullptr);
   learned_update_forms(L, s, k, st);
   k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k,
                                         nullptr, nullptr, 0);
-  k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
+  // soma pushes: by the next tick's prologue within a graph, here on its last tick
+  if (last)
+    k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
                                        nullptr, nullptr, 0, s.ctl, k);
   if (features_on && L.T)
     k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.cap, L.part,
@@ -1151,7 +1119,8 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return (int32_t)e;
     cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true);
-    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = learned_tick(*L, *s, k, features_on, L->capture);
+    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++)
+      le = learned_tick(*L, *s, k, k + 1 == tpg, features_on, L->capture);
     if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(L->capture, &g);

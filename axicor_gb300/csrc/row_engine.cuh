@@ -935,7 +935,7 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
                                                    const uint32_t* __restrict__ wcnt, uint32_t nwu,
                                                    uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl, uint32_t k,
                                                    uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
-  if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
+  (void)lc;   // the learned engine lists its sparse ticks' spikers here too
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
@@ -1028,7 +1028,7 @@ __global__ void __launch_bounds__(256) k_rows_gsop_rows(ShardVramPtrs P, uint32_
                                                         const uint32_t* __restrict__ wcnt, uint32_t nwu,
                                                         uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
                                                         uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
-  if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: a sparse tick
+  (void)lc;   // the learned engine lists its sparse ticks' spikers here too
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
