@@ -886,7 +886,7 @@ static cudaError_t learned_index(Learned& L, cudaStream_t st) {
 
 // The update forms of one tick: the dense update (it returns at once on a
 // sparse tick that did not overflow) and the sparse kernels (they return at
-// once on a dense tick).
+// once on a dense tick), then the GSOP passes over the spikers either listed.
 static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, cudaStream_t st) {
   RowCache& r = *s.rows;
   const uint32_t N = L.N, A = L.A;
@@ -899,6 +899,8 @@ static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, cudaSt
   // 4 blocks of 256 per SM: the 32 warps per SM whose slices the GSOP passes read
   k_learn_update<<<4 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, r.lfz, r.gs_n, r.gd_n, r.wcnt,
                                           s.ctl, k);
+  // GSOP of the spikers listed by whichever form ran
+  launch_rows_gsop(L.v, s, A, k, fix_cap, st);
 }
 
 // One tick: schedule, prologue, both update forms (the one not picked returns

@@ -1298,33 +1298,42 @@ static size_t lit_smem_limit() {
   return limit;
 }
 
-// The update pass (with the fully-lit bitmap in shared memory when it fits)
-// and the GSOP pass over the spikers it listed.  lc: the learned engine's
-// control block (both return at once on its sparse ticks), or null.
+// The update pass (with the fully-lit bitmap in shared memory when it fits).
+// lc: the learned engine's control block (the pass returns at once on its
+// sparse ticks), or null.
+static bool rows_lit(uint32_t A) { return ((size_t)(A >> 5) + 1) * 4 <= lit_smem_limit(); }
+
 static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, uint32_t k,
-                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream,
-                               cudaEvent_t after_update = nullptr) {
+                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream) {
   RowCache& r = *s.rows;
   const int sms = sm_count();
-  const size_t lit_bytes = ((size_t)(A >> 5) + 1) * 4;
-  const uint32_t nwu = (uint32_t)sms * 32u;   // both variants: 32 warps per SM; the GSOP pass: a warp per
-                                               // update warp's segment
-  if (lit_bytes <= lit_smem_limit()) {
-    k_rows_update<true><<<sms, 1024, lit_bytes, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                        s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt);
-    if (after_update) cudaEventRecord(after_update, stream);
-    k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
-                                                   nwu, r.fix, s.ctl, k, fix_cap, lc);
-    k_rows_gsop_rows<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
-                                                        r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap, lc);
-  } else {
+  if (rows_lit(A))
+    k_rows_update<true><<<sms, 1024, ((size_t)(A >> 5) + 1) * 4, stream>>>(
+        v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
+        r.lfz, r.wcnt);
+  else
     k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                       s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt);
-    if (after_update) cudaEventRecord(after_update, stream);
+}
+
+// The GSOP passes over the spikers the tick's update pass listed (32 warps per
+// SM, each with its slice of the evaluated list; a GSOP warp per slice).
+static void launch_rows_gsop(const ShardVramPtrs& v, ShardScratch& s, uint32_t A, uint32_t k, uint32_t fix_cap,
+                             cudaStream_t stream) {
+  RowCache& r = *s.rows;
+  const uint32_t nwu = (uint32_t)sm_count() * 32u;
+  if (rows_lit(A)) {
+    k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
+                                                   nwu, r.fix, s.ctl, k, fix_cap, nullptr);
+    k_rows_gsop_rows<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
+                                                        r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap,
+                                                        nullptr);
+  } else {
     k_rows_gsop<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
-                                                    nwu, r.fix, s.ctl, k, fix_cap, lc);
+                                                    nwu, r.fix, s.ctl, k, fix_cap, nullptr);
     k_rows_gsop_rows<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
-                                                         r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap, lc);
+                                                         r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap,
+                                                         nullptr);
   }
 }
 
@@ -1344,7 +1353,9 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
         raise, r.lit, LearnDev{}, a.k > 0 ? s.pend : nullptr);
   if (ev) cudaEventRecord(ev[2], stream);
   // stages: ev[2]..ev[3] the update pass, ev[3]..ev[4] the GSOP passes, fix-up and push
-  launch_rows_update(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream, ev ? ev[3] : nullptr);
+  launch_rows_update(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream);
+  if (ev) cudaEventRecord(ev[3], stream);
+  launch_rows_gsop(v, s, A, a.k, min(a.fix_cap, kFixCap), stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
                                             a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0);
