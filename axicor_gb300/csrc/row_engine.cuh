@@ -919,9 +919,9 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
 }
 
 // ---------------------------------------------------------------------------
-// per tick 2b: GSOP (physics.cu:281-373) of the listed spikers, a thread per
-// spiker, over the slots of amask only (the others are frozen: GSOP leaves
-// them as they are).  Each slot is classified as in the update pass (fully lit,
+// per tick 2b: GSOP (physics.cu:281-373) of the listed spikers over the slots
+// of amask only (the others are frozen: GSOP leaves them as they are), the
+// (spiker, slot) items of 32 spikers spread over the warp's lanes.  Each slot is classified as in the update pass (fully lit,
 // else the tick's hit masks; exact path for segments >= 31, other lengths,
 // several owners, or a hit that one same-tick push could change) and updated
 // from the gtab deltas, on the exact path, or deferred to the fix-up stage.
@@ -954,62 +954,84 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
   for (uint32_t uw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; uw < nwu; uw += ngw) {
     const uint32_t cntw = wcnt[uw];
     const uint32_t beg = min(uw * per_warp, ecount);
-    for (uint32_t e = lane; e < cntw; e += 32) {
-      const uint32_t n = gs_n[beg + e];
-      const uint8_t flags = P.soma_flags[n];
-      const uint32_t c = cnt[n] & 0xFFu;
-      const uint32_t var = flags >> 4;
-      const VariantParameters& p = lut[var];
-      const uint32_t prop = p.signal_propagation_length;
-      const bool exact = prop == s_pmax;
-      const bool gfast = exact && prop <= 16u;
-      const uint4 am = amask[n];
-      const uint32_t words[4] = {am.x, am.y, am.z, am.w};
-      gdone += c - (__popc(am.x) + __popc(am.y) + __popc(am.z) + __popc(am.w));   // frozen slots
+    for (uint32_t e0 = 0; e0 < cntw; e0 += 32) {
+      // 32 listed spikers; their movable slots are spread over the lanes
+      const bool has = e0 + lane < cntw;
+      const uint32_t my_n = has ? gs_n[beg + e0 + lane] : 0u;
+      const uint4 my_am = has ? amask[my_n] : make_uint4(0, 0, 0, 0);
+      const uint32_t my_k = __popc(my_am.x) + __popc(my_am.y) + __popc(my_am.z) + __popc(my_am.w);
+      if (has) gdone += (cnt[my_n] & 0xFFu) - my_k;   // frozen slots: GSOP leaves them as they are
+      uint32_t incl = my_k;   // inclusive prefix of the slot counts over the lanes
 #pragma unroll
-      for (int wq = 0; wq < 4; wq++) {
-        uint32_t rest = words[wq];
-        while (rest) {
-          const uint32_t q = 32u * wq + (__ffs(rest) - 1);
-          rest &= rest - 1u;
-          const size_t r = (size_t)n * kRowStride + q;
-          const uint32_t t = __ldg(rt + r);
-          const int16_t w16 = rw[r];
-          const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;
-          const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
-          bool hit, fast;
-          if (LIT && gfast && (s - 1u) < seg_hi && ((__ldg(lit_bits + (ax >> 5)) >> (ax & 31u)) & 1u)) {
-            hit = true;
-            fast = true;
-          } else {
-            const uint2 m = __ldg(mask2 + ax);
-            const uint32_t sh = min(s, 31u);
-            const uint32_t bx = (m.x >> sh) & 1u, by = (m.y >> sh) & 1u;
-            hit = (bx | by) != 0u;
-            if (hit && (s >= 31u || !exact)) hit = hit_exact(P.axon_heads, A, ax, s, prop);
-            fast = gfast && s < 31u && !(m.y >> 31) && (bx || by == (s == 0u));
-          }
-          int16_t nw = w16;
-          if (fast) {
-            const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
-            const int2 d = gtab[var][min((uint32_t)aw >> 11, 15u)];
-            int32_t na = aw + (hit ? d.x : -d.y);
-            na = min(max(na, 0), 32767);
-            nw = (int16_t)(w16 < 0 ? -na : na);
-            gdone++;
-          } else {
-            const int res = gsop_general(P.axon_heads, mask2, A, ax, s, p, flags, dopamine, &nw);
-            if (res == 2) continue;
-            gdone++;
-            if (res == 1) {
-              const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
-              if (slot < fix_cap) fix[slot] = (uint32_t)r;
-              else ctl->fix_overflow = 1u;
-              continue;
-            }
-          }
-          if (nw != w16) rw[r] = nw;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(kFull, incl, o);
+        if (lane >= (uint32_t)o) incl += x;
+      }
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      for (uint32_t it0 = 0; it0 < total; it0 += 32) {   // warp-uniform: every lane takes part in the shuffles
+        const uint32_t it = it0 + lane;
+        // the lane that owns item it: the first whose inclusive prefix exceeds it
+        uint32_t owner = 0;
+#pragma unroll
+        for (int stp = 16; stp > 0; stp >>= 1) {
+          const uint32_t v = __shfl_sync(kFull, incl, owner + stp - 1);
+          if (v <= it) owner += stp;
         }
+        owner = min(owner, 31u);
+        const uint32_t n = __shfl_sync(kFull, my_n, owner);
+        const uint32_t prev = __shfl_sync(kFull, incl - my_k, owner);
+        const uint32_t am0 = __shfl_sync(kFull, my_am.x, owner), am1 = __shfl_sync(kFull, my_am.y, owner);
+        const uint32_t am2 = __shfl_sync(kFull, my_am.z, owner), am3 = __shfl_sync(kFull, my_am.w, owner);
+        if (it >= total) continue;
+        uint32_t rank = it - prev, q;   // the rank-th set bit of the owner's mask
+        const uint32_t c0 = __popc(am0), c1 = __popc(am1), c2 = __popc(am2);
+        if (rank < c0) q = __fns(am0, 0, rank + 1);
+        else if ((rank -= c0) < c1) q = 32u + __fns(am1, 0, rank + 1);
+        else if ((rank -= c1) < c2) q = 64u + __fns(am2, 0, rank + 1);
+        else q = 96u + __fns(am3, 0, rank - c2 + 1);
+        const uint8_t flags = P.soma_flags[n];
+        const uint32_t var = flags >> 4;
+        const VariantParameters& p = lut[var];
+        const uint32_t prop = p.signal_propagation_length;
+        const bool exact = prop == s_pmax;
+        const bool gfast = exact && prop <= 16u;
+        const size_t r = (size_t)n * kRowStride + q;
+        const uint32_t t = __ldg(rt + r);
+        const int16_t w16 = rw[r];
+        const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;
+        const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+        bool hit, fast;
+        if (LIT && gfast && (s - 1u) < seg_hi && ((__ldg(lit_bits + (ax >> 5)) >> (ax & 31u)) & 1u)) {
+          hit = true;
+          fast = true;
+        } else {
+          const uint2 m = __ldg(mask2 + ax);
+          const uint32_t sh = min(s, 31u);
+          const uint32_t bx = (m.x >> sh) & 1u, by = (m.y >> sh) & 1u;
+          hit = (bx | by) != 0u;
+          if (hit && (s >= 31u || !exact)) hit = hit_exact(P.axon_heads, A, ax, s, prop);
+          fast = gfast && s < 31u && !(m.y >> 31) && (bx || by == (s == 0u));
+        }
+        int16_t nw = w16;
+        if (fast) {
+          const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+          const int2 d = gtab[var][min((uint32_t)aw >> 11, 15u)];
+          int32_t na = aw + (hit ? d.x : -d.y);
+          na = min(max(na, 0), 32767);
+          nw = (int16_t)(w16 < 0 ? -na : na);
+          gdone++;
+        } else {
+          const int res = gsop_general(P.axon_heads, mask2, A, ax, s, p, flags, dopamine, &nw);
+          if (res == 2) continue;
+          gdone++;
+          if (res == 1) {
+            const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+            if (slot < fix_cap) fix[slot] = (uint32_t)r;
+            else ctl->fix_overflow = 1u;
+            continue;
+          }
+        }
+        if (nw != w16) rw[r] = nw;
       }
     }
   }
