@@ -40,8 +40,9 @@ struct RowCache {
   uint32_t* lit = nullptr;  // [A/32+1] fully-lit axons of the tick, one bit each
   uint32_t* gs_n = nullptr; // [N] spikers with 1..8 slots GSOP may move (a thread each)
   uint32_t* gd_n = nullptr; // [N] spikers with more (8 lanes each)
-  uint4* amask = nullptr;   // [N] slots (bit q) whose weights GSOP may move (set at batch start)
+  uint4* amask = nullptr;   // [N] row positions (bit q) whose weights GSOP may move (set at batch start)
   uint8_t* lfz = nullptr;   // [N] number of those slots (set at batch start)
+  uint4* omask = nullptr;   // [N] columnar slots placed first in the row (the movable ones; all when unpermuted)
   uint32_t* wcnt = nullptr; // [2][kMaxUpdateWarps] spikers each warp of the update pass listed (gs_n, gd_n)
 };
 
@@ -71,7 +72,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix = 
 void rows_free(ShardScratch& s);
 // row_sum: also compute the targets checksum (ShardCtl::row_sum) the learned engine checks its index against.
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
-                              bool row_sum = false);
+                              bool row_sum = false, bool permute = true);
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream);
 
 // Registry keyed by the axon_heads pointer.  Created by cu_allocate_shard;

@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(256) k_learn_update(ShardVramPtrs P, LearnDev 
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
       if (spike) {
         nspk++;
-        if (lf == 0u) gdone += cw & 0xFFu;   // every weight of the row is frozen
+        if (lf <= 8u) gdone += (cw & 0xFFu) - lf;   // frozen slots of rows k_rows_gsop takes, or all
         const uint32_t my_axon = P.soma_to_axon[n];
         if (my_axon != AXC_NO_AXON) {
           if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
@@ -843,7 +843,7 @@ static cudaError_t learned_index(Learned& L, cudaStream_t st) {
   if (!s) return e;
   e = rows_alloc(*s, L.N, L.A);
   if (e != cudaSuccess) return e;
-  e = launch_rows_begin(L.v, *s, L.N, L.A, st, true);
+  e = launch_rows_begin(L.v, *s, L.N, L.A, st, true, false);
   if (e != cudaSuccess) return e;
   const RowCache& r = *s->rows;
   e = cudaMemsetAsync(L.deg, 0, (size_t)L.A * 4, st);
@@ -893,7 +893,7 @@ static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, cudaSt
   const int sms = sm_count();
   const LearnDev D = L.dev();
   const uint32_t fix_cap = kFixCap;
-  launch_rows_update(L.v, s, N, A, k, fix_cap, L.ctl, st);
+  launch_rows_update<false>(L.v, s, N, A, k, fix_cap, L.ctl, st);
   k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw,
                                                                 L.v.soma_flags, L.v.axon_heads, A, L.acc, s.ctl);
   // 4 blocks of 256 per SM: the 32 warps per SM whose slices the GSOP passes read
@@ -1120,7 +1120,7 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   } else {
     e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return (int32_t)e;
-    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true);
+    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true, false);
     for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++)
       le = learned_tick(*L, *s, k, k + 1 == tpg, features_on, L->capture);
     if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);

@@ -8,28 +8,34 @@
 // the spikers' slots with one sector per slot.  For the length of one batch the
 // engine keeps a neuron-major copy ([neuron][128]) of targets and weights:
 //
-//   batch start  k_rows_build      columnar -> rows, first-empty count per neuron
-//                k_rows_mult       somas per axon (soma_to_axon multiplicity)
-//   per tick     k_rows_prologue   axon pushes + propagation + split masks,
+//   batch start  k_rows_mult       somas per axon (soma_to_axon multiplicity)
+//                k_rows_build      columnar -> rows (the slots whose weights may
+//                                  still move first), per-neuron counts and masks
+//   per tick     k_rows_prologue   the previous tick's soma pushes, axon pushes +
+//                                  propagation + split masks, fully-lit bitmap,
 //                                  refractory countdown, list of evaluated neurons
-//                k_rows_update     8 lanes per evaluated neuron: gather/sum, GLIF,
-//                                  and GSOP in the same pass on the rows in registers
-//                k_rows_fixup      the GSOP slots whose result depends on same-tick pushes
-//                k_push            soma pushes, readout (shared with the columnar path)
-//   batch end    k_rows_writeback  weights rows -> columnar (slots before the first empty)
+//                k_rows_update     8 lanes per evaluated neuron: gather/sum, GLIF;
+//                                  lists the spikers with movable slots
+//                k_rows_gsop       GSOP of spikers with 1..8 movable slots
+//                k_rows_gsop_rows  GSOP of spikers with more, 8 lanes per row
+//                k_rows_fixup      readout, the GSOP slots whose result depends on
+//                                  same-tick pushes
+//                k_rows_push       the spikers' pushes (a batch's last tick only;
+//                                  otherwise the next prologue applies them)
+//   batch end    k_rows_writeback  weights rows -> columnar
 //
-// GSOP in the update pass.  GSOP must see the heads after this tick's soma
-// pushes (physics.cu:281-373 runs after the update kernel), which are not all
-// known while neurons are still being updated.  A push inserts a 0 head and
-// drops h7, so for an axon owned by one soma the result can only change when
-// segment 0 is involved or h7 is the only head in the tail.  The axon stage
-// writes two masks per axon — hits of heads 0..6 and hits of head 7 — so the
-// update pass knows, per slot, the "no push" and "one push" outcomes.  When
-// they agree the weight is updated at once; otherwise the slot is left
-// untouched and listed, and k_rows_fixup applies it with the actual push count
-// (and from the original weight).  Axons owned by two or more somas, variants
-// whose length differs from the LUT maximum or exceeds 16 (where the cooling
-// shift can be non-zero) and segments >= 31 take the exact general path.
+// GSOP against same-tick pushes.  GSOP must see the heads after this tick's
+// soma pushes (physics.cu:281-373 runs after the update kernel).  A push
+// inserts a 0 head and drops h7, so for an axon owned by one soma the result
+// can only change when segment 0 is involved or h7 is the only head in the
+// tail.  The axon stage writes two masks per axon — hits of heads 0..6 and
+// hits of head 7 — so GSOP knows, per slot, the "no push" and "one push"
+// outcomes.  When they agree the weight is updated at once; otherwise the slot
+// is left untouched and listed, and k_rows_fixup applies it with the actual
+// push count (and from the original weight).  Axons owned by two or more
+// somas, variants whose length differs from the LUT maximum or exceeds 16
+// (where the cooling shift can be non-zero) and segments >= 31 take the exact
+// general path.
 
 namespace axc {
 namespace {
@@ -196,9 +202,7 @@ __device__ __forceinline__ unsigned long long slot_mix(uint32_t t, uint32_t r) {
 }
 
 // ---------------------------------------------------------------------------
-// batch start: columnar -> neuron-major, first-empty counts.
-// 32 neurons per 256-thread block; rows are read 8 at a time until every
-// neuron of the tile has met its first empty target.
+// batch start / end: the row copy
 // ---------------------------------------------------------------------------
 // Smallest |w| from which every inertia rank of variant v is 0 (0x10000:
 // none): GSOP moves such a weight by 0 whatever the hit, distance, burst or
@@ -210,11 +214,41 @@ __device__ __forceinline__ int32_t frozen_from(const VariantParameters& p) {
   return r0 < 16 ? r0 * 2048 : 0x10000;
 }
 
+// thr <= |w| <= 32767, in plain signed comparisons (-32768 is not frozen: the
+// clamp moves it).
+__device__ __forceinline__ bool frozen_weight(int16_t w16, int32_t thr) {
+  const int32_t w = w16;
+  return w != -32768 && (w >= thr || w <= -thr);
+}
+
+// Row position of columnar slot q (lane = q & 31) when the slots of mask o
+// come first, in slot order, and the others follow in slot order: word = the
+// 32 bits of o holding q, pre = set bits of o before that word, lf = set bits
+// of o in all.
+__device__ __forceinline__ uint32_t row_pos(uint32_t word, uint32_t lane, uint32_t q, uint32_t pre, uint32_t lf) {
+  const uint32_t below = pre + __popc(word & ((1u << lane) - 1u));
+  return ((word >> lane) & 1u) ? below : lf + q - below;
+}
+
+// Batch start: columnar -> rows.  32 neurons per 256-thread block; the
+// columns are read 8 slots at a time until every neuron of the tile has met
+// its first empty target.  A slot whose weight GSOP may still move (not
+// frozen_weight, or any slot of a row with an invalid target) is movable;
+// weights only freeze, so the marks hold for the whole batch.  With permute
+// the movable slots go first in the row, then the others (each group in slot
+// order), so that GSOP reads a short prefix of the row; the dendrite sum (a
+// wrapping i32 sum) and GSOP (per slot) do not depend on the order.
+// Per neuron: cnt = used slots (| kRowBad), lfz = movable slots, amask = their
+// row positions, omask = the columnar slots placed first (read by the
+// write-back; every used slot when the row keeps the columnar order).
 __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__ targets,
-                                                    const int16_t* __restrict__ weights, uint32_t N,
+                                                    const int16_t* __restrict__ weights,
+                                                    const uint8_t* __restrict__ flags, uint32_t N,
                                                     uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
-                                                    uint16_t* __restrict__ cnt, ShardCtl* __restrict__ ctl, uint32_t A,
-                                                    uint32_t want_sum) {
+                                                    uint16_t* __restrict__ cnt, uint4* __restrict__ amask,
+                                                    uint4* __restrict__ omask, uint8_t* __restrict__ lfz,
+                                                    ShardCtl* __restrict__ ctl, uint32_t A, uint32_t want_sum,
+                                                    uint32_t permute) {
   __shared__ uint32_t s_t[AXC_MAX_DENDRITES][33];
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_cnt[32];
@@ -248,27 +282,63 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     const uint32_t n = n0 + j;
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
+    const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
     bool bad = false;
     uint32_t smx = 0;
     unsigned long long hsum = 0;
-    for (uint32_t q = lane; q < c; q += 32) {
-      uint32_t t = s_t[q][j];
-      // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
-      // which sends the slot down the exact path (hit_exact / gsop_general skip it)
-      if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
-        t = (t & ~AXC_TARGET_AXON_MASK) | (A + 1u);
-        bad = true;
+    uint32_t mv[4], all[4];   // movable / used slots, by columnar position
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) {
+      const uint32_t q = 32u * ch + lane;
+      bool mov = false;
+      if (q < c) {
+        uint32_t t = s_t[q][j];
+        // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
+        // which sends the slot down the exact path (hit_exact / gsop_general skip it)
+        if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
+          t = (t & ~AXC_TARGET_AXON_MASK) | (A + 1u);
+          s_t[q][j] = t;
+          bad = true;
+        }
+        smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
+        if (want_sum) hsum += slot_mix(t, n * kRowStride + q);
+        mov = !frozen_weight(s_w[q][j], fz);
       }
-      smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
-      if (want_sum) hsum += slot_mix(t, n * kRowStride + q);
-      rt[(size_t)n * kRowStride + q] = t;
-      rw[(size_t)n * kRowStride + q] = s_w[q][j];
+      mv[ch] = __ballot_sync(kFull, mov);
+      all[ch] = __ballot_sync(kFull, q < c);
     }
     bad = __any_sync(kFull, bad);
     smx = __reduce_max_sync(kFull, smx);
     if (want_sum) hsum = warp_sum(hsum);
+    if (bad) {
+#pragma unroll
+      for (int ch = 0; ch < 4; ch++) mv[ch] = all[ch];
+    }
+    const uint32_t lf = __popc(mv[0]) + __popc(mv[1]) + __popc(mv[2]) + __popc(mv[3]);
+    // placement: the movable slots first (permute), else every used slot (identity)
+    uint32_t o[4];
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) o[ch] = permute ? mv[ch] : all[ch];
+    const uint32_t olf = permute ? lf : c;
+    uint32_t pre = 0, am[4];
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) {
+      const uint32_t q = 32u * ch + lane;
+      const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
+      pre += __popc(o[ch]);
+      if (q < c) {
+        rt[(size_t)n * kRowStride + pos] = s_t[q][j];
+        rw[(size_t)n * kRowStride + pos] = s_w[q][j];
+      }
+      // the movable slots by row position: the first lf positions, or mv itself
+      const uint32_t lo = 32u * ch;
+      am[ch] = permute ? (lf >= lo + 32u ? kFull : (lf > lo ? (1u << (lf - lo)) - 1u : 0u)) : mv[ch];
+    }
     if (lane == 0) {
       cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
+      amask[n] = make_uint4(am[0], am[1], am[2], am[3]);
+      omask[n] = make_uint4(o[0], o[1], o[2], o[3]);
+      lfz[n] = (uint8_t)lf;
       if (c) {
         wc = max(wc, c);
         ws = max(ws, smx);
@@ -303,10 +373,12 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
   if (a < A) atomicAdd(&mult[a], 1u);
 }
 
-// batch end: weights rows -> columnar for slots before the first empty target.
+// batch end: weights rows -> columnar for the slots before the first empty
+// target (slot q of neuron n from row position row_pos of its omask).
 __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ weights, uint32_t N,
                                                         const int16_t* __restrict__ rw,
-                                                        const uint16_t* __restrict__ cnt) {
+                                                        const uint16_t* __restrict__ cnt,
+                                                        const uint4* __restrict__ omask) {
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_c[32];
   const uint32_t n0 = blockIdx.x * 32;
@@ -315,7 +387,18 @@ __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ we
     const uint32_t n = n0 + j;
     const uint32_t c = n < N ? (cnt[n] & 0xFFu) : 0u;
     if (lane == 0) s_c[j] = c;
-    for (uint32_t q = lane; q < c; q += 32) s_w[q][j] = rw[(size_t)n * kRowStride + q];
+    if (c == 0) continue;
+    const uint4 om = omask[n];
+    const uint32_t o[4] = {om.x, om.y, om.z, om.w};
+    const uint32_t olf = __popc(om.x) + __popc(om.y) + __popc(om.z) + __popc(om.w);
+    uint32_t pre = 0;
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) {
+      const uint32_t q = 32u * ch + lane;
+      const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
+      pre += __popc(o[ch]);
+      if (q < c) s_w[q][j] = rw[(size_t)n * kRowStride + pos];
+    }
   }
   __syncthreads();
   uint32_t cmax = 0;
@@ -566,46 +649,6 @@ __device__ __forceinline__ void row_load(uint4 (&T)[4], uint2 (&W)[4], const uin
   }
 }
 
-// thr <= |w| <= 32767, in plain signed comparisons (-32768 is not frozen: the
-// clamp moves it).
-__device__ __forceinline__ bool frozen_weight(int16_t w16, int32_t thr) {
-  const int32_t w = w16;
-  return w != -32768 && (w >= thr || w <= -thr);
-}
-
-// batch start, after the row copy: bit q of amask[n] is set when the weight
-// of live slot q may still move under GSOP (not frozen_weight, or the row
-// holds an invalid target); lfz[n] = the number of such slots.  Weights only
-// freeze, so both hold for the whole batch.  A thread per (neuron, 16-slot
-// chunk).
-__global__ void __launch_bounds__(256) k_rows_lanes(const int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
-                                                    const uint8_t* __restrict__ flags, uint32_t N,
-                                                    uint4* __restrict__ amask, uint8_t* __restrict__ lfz) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t n = t >> 3, part = t & 7u;   // slots 16 part .. 16 part + 15
-  uint32_t bits = 0;
-  if (n < N) {
-    const uint32_t cw = cnt[n], c = cw & 0xFFu;
-    const bool all = (cw & kRowBad) != 0u;
-    const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
-    const int16_t* rw_n = rw + (size_t)n * kRowStride + 16u * part;
-#pragma unroll
-    for (int i = 0; i < 16; i++) {
-      const uint32_t q = 16u * part + i;
-      if (q < c && (all || !frozen_weight(rw_n[i], fz))) bits |= 1u << (q & 31u);
-    }
-  }
-  // word w of the neuron = the two 16-slot chunks 2w and 2w+1
-  const uint32_t other = __shfl_xor_sync(kFull, bits, 1);
-  const uint32_t word = bits | other;
-  const uint32_t w0 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 0), w1 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 2);
-  const uint32_t w2 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 4), w3 = __shfl_sync(kFull, word, (threadIdx.x & 24u) + 6);
-  if (part == 0 && n < N) {
-    amask[n] = make_uint4(w0, w1, w2, w3);
-    lfz[n] = (uint8_t)(__popc(w0) + __popc(w1) + __popc(w2) + __popc(w3));
-  }
-}
-
 // The dendrite pass over the slots one lane holds (row_shape) of a row with c
 // used slots: returns the lane's share of the input current and sets, per slot
 // (bit 4j+i; single-slot round t: bit 12+t), hitb = the segment is hit and
@@ -812,7 +855,10 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
 // LIT: 1024-thread blocks (one per SM) that first copy the prologue's
 // fully-lit bitmap (one bit per axon) into shared memory; slots whose axon is
 // fully lit need no mask gather from L2.
-template <bool LIT>
+// INLINE (rows with their movable slots first): GSOP of each spiker's movable
+// slots on the weights still in registers; else the spikers with movable
+// slots are listed for k_rows_gsop / k_rows_gsop_rows.
+template <bool LIT, bool INLINE>
 __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
     k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A, const uint32_t* __restrict__ rt,
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
@@ -821,6 +867,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint32_t* __restrict__ gd_n,
                   const uint8_t* __restrict__ lfz, uint32_t* __restrict__ wcnt) {
   __shared__ VariantParameters lut[16];
+  __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
   extern __shared__ uint32_t s_lit[];
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
@@ -831,6 +878,11 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
     for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) s_lit[w] = __ldg(lit_bits + w);
   }
   __syncthreads();
+  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
+  if (INLINE) {
+    build_gtab(gtab, lut, dopamine);
+    __syncthreads();
+  }
   const uint32_t tick = ctl->tick_base + k;
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t smax = ctl->row_smax;   // longest row of the shard: rows are loaded up to here
@@ -895,12 +947,22 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
           }
         }
       }
+      if (INLINE) {
+        // GSOP (physics.cu:281-373) of the spiker's movable slots, the first lf
+        // of its row; frozen slots (GSOP leaves them as they are) are counted
+        if (spike && lf > 0u)
+          gdone += row_gsop(W, hitb, slowb, lf, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
+                            dopamine, ctl, fix, fix_cap, n);
+        if (spike && g8 == 0) gdone += c - lf;
+        continue;
+      }
       // GSOP (physics.cu:281-373) runs in k_rows_gsop / k_rows_gsop_rows over
       // the spikers listed here (those with slots that may move: a few, or
-      // many), in this warp's segments of the lists; a fully frozen row is only
-      // counted
+      // many), in this warp's segments of the lists; frozen slots (GSOP leaves
+      // them as they are) of a row with a few movable ones or none are only
+      // counted here
       const bool few = spike && lf > 0u && lf <= 8u, many = spike && lf > 8u;
-      if (spike && lf == 0u && g8 == 0) gdone += c;
+      if (spike && lf <= 8u && g8 == 0) gdone += c - lf;
       const uint32_t ab = __ballot_sync(kFull, few && g8 == 0), db = __ballot_sync(kFull, many && g8 == 0);
       if (few && g8 == 0) gs_n[beg + wc + __popc(ab & ((1u << lane) - 1u))] = n;
       if (many && g8 == 0) gd_n[beg + wd + __popc(db & ((1u << lane) - 1u))] = n;
@@ -908,7 +970,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       wd += __popc(db);
     }
   }
-  if (lane == 0) {
+  if (!INLINE && lane == 0) {
     wcnt[wid] = wc;
     wcnt[kMaxUpdateWarps + wid] = wd;
   }
@@ -960,7 +1022,6 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
       const uint32_t my_n = has ? gs_n[beg + e0 + lane] : 0u;
       const uint4 my_am = has ? amask[my_n] : make_uint4(0, 0, 0, 0);
       const uint32_t my_k = __popc(my_am.x) + __popc(my_am.y) + __popc(my_am.z) + __popc(my_am.w);
-      if (has) gdone += (cnt[my_n] & 0xFFu) - my_k;   // frozen slots: GSOP leaves them as they are
       uint32_t incl = my_k;   // inclusive prefix of the slot counts over the lanes
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -1251,6 +1312,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_gdn = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_am = off; off = al(off + (size_t)N * 16 + 16);
   const size_t o_lfz = off; off = al(off + (size_t)N + 4);
+  const size_t o_om = off; off = al(off + (size_t)N * 16 + 16);
   const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 8);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
@@ -1274,6 +1336,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->gd_n = reinterpret_cast<uint32_t*>(b + o_gdn);
   r->amask = reinterpret_cast<uint4*>(b + o_am);
   r->lfz = reinterpret_cast<uint8_t*>(b + o_lfz);
+  r->omask = reinterpret_cast<uint4*>(b + o_om);
   r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
   s.rows = r;
   return cudaSuccess;
@@ -1287,16 +1350,16 @@ void rows_free(ShardScratch& s) {
 }
 
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
-                              bool row_sum) {
+                              bool row_sum, bool permute) {
   RowCache& r = *s.rows;
   k_rows_reset_lists<<<1, 1, 0, stream>>>(s.ctl);
   cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
   if (e != cudaSuccess) return e;
   if (N) {
     k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
-    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, N, r.rt, r.rw, r.cnt,
-                                                    s.ctl, A, row_sum ? 1u : 0u);
-    k_rows_lanes<<<(N * 8 + 255) / 256, 256, 0, stream>>>(r.rw, r.cnt, v.soma_flags, N, r.amask, r.lfz);
+    k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, v.soma_flags, N, r.rt,
+                                                    r.rw, r.cnt, r.amask, r.omask, r.lfz, s.ctl, A,
+                                                    row_sum ? 1u : 0u, permute ? 1u : 0u);
   }
   return cudaGetLastError();
 }
@@ -1311,7 +1374,10 @@ static size_t lit_smem_limit() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     size_t lim = optin > 8192 ? (size_t)optin - 8192 : 0;
-    if (cudaFuncSetAttribute(k_rows_update<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) != cudaSuccess) {
+    if (cudaFuncSetAttribute(k_rows_update<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_rows_update<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) !=
+            cudaSuccess) {
       cudaGetLastError();
       lim = 0;
     }
@@ -1325,17 +1391,21 @@ static size_t lit_smem_limit() {
 // sparse ticks), or null.
 static bool rows_lit(uint32_t A) { return ((size_t)(A >> 5) + 1) * 4 <= lit_smem_limit(); }
 
+// inline: GSOP inside the pass (rows with their movable slots first), else
+// the spikers are listed for launch_rows_gsop.
+template <bool INLINE>
 static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, uint32_t k,
                                uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream) {
   RowCache& r = *s.rows;
   const int sms = sm_count();
   if (rows_lit(A))
-    k_rows_update<true><<<sms, 1024, ((size_t)(A >> 5) + 1) * 4, stream>>>(
+    k_rows_update<true, INLINE><<<sms, 1024, ((size_t)(A >> 5) + 1) * 4, stream>>>(
         v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
         r.lfz, r.wcnt);
   else
-    k_rows_update<false><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                      s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt);
+    k_rows_update<false, INLINE><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend,
+                                                              r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
+                                                              r.lfz, r.wcnt);
 }
 
 // The GSOP passes over the spikers the tick's update pass listed (32 warps per
@@ -1374,10 +1444,9 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
         raise, r.lit, LearnDev{}, a.k > 0 ? s.pend : nullptr);
   if (ev) cudaEventRecord(ev[2], stream);
-  // stages: ev[2]..ev[3] the update pass, ev[3]..ev[4] the GSOP passes, fix-up and push
-  launch_rows_update(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream);
+  // stages: ev[2]..ev[3] the update pass with GSOP, ev[3]..ev[4] fix-up and push
+  launch_rows_update<true>(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream);
   if (ev) cudaEventRecord(ev[3], stream);
-  launch_rows_gsop(v, s, A, a.k, min(a.fix_cap, kFixCap), stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
                                             a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0);
@@ -1394,7 +1463,7 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
 
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream) {
   RowCache& r = *s.rows;
-  if (N) k_rows_writeback<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_weights, N, r.rw, r.cnt);
+  if (N) k_rows_writeback<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_weights, N, r.rw, r.cnt, r.omask);
   return cudaGetLastError();
 }
 
