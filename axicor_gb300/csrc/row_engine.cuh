@@ -674,14 +674,23 @@ __device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&
       lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
       m[i] = (q0 + i < c && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
     }
+    uint32_t need = 0;   // live slots off the fully-lit path
 #pragma unroll
     for (int i = 0; i < 4; i++) {
       if (q0 + i >= c) continue;
       if (LIT && lit[i]) {                      // segment 1..30 of a fully lit axon: hit, fast GSOP
         i_in = wadd(i_in, (int32_t)half_of(W[j], i));
         hitb |= 1u << (4 * j + i);
-        continue;
+      } else {
+        need |= 1u << i;
       }
+    }
+    // warp-uniform: most rounds have every slot of the warp's four rows on the
+    // fully-lit path, and skip the mask path as a whole
+    if (LIT && !__any_sync(kFull, need)) continue;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if (!((need >> i) & 1u)) continue;
       const uint32_t t = word_of(T[j], i);
       const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
       const uint32_t sh = min(s, 31u);
@@ -699,32 +708,43 @@ __device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&
     }
   }
   if (sh.F < 4u) {
+    // single-slot tail rounds t = 0, 1: slot 32F + g8 + 8t, bit 12 + t
+    uint2 m[2];
+    uint32_t need = 0;
 #pragma unroll
     for (int t = 0; t < 2; t++) {
-      if ((uint32_t)t >= sh.TR) continue;
+      m[t] = make_uint2(0, 0);
       const uint32_t q = 32u * sh.F + g8 + 8u * t;
-      if (q >= c) continue;
+      if ((uint32_t)t >= sh.TR || q >= c) continue;
       const uint32_t tw = t ? T[3].y : T[3].x;
       const uint32_t ax = (tw & AXC_TARGET_AXON_MASK) - 1u;
-      const uint32_t b = 1u << (12 + t);
-      const int32_t w = (int32_t)half_of(W[3], t);
       if (LIT && gfast && ((tw >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u)) {
-        i_in = wadd(i_in, w);
-        hitb |= b;
-        continue;
+        i_in = wadd(i_in, (int32_t)half_of(W[3], t));
+        hitb |= 1u << (12 + t);
+      } else {
+        m[t] = __ldg(mask2 + ax);
+        need |= 1u << t;
       }
-      const uint2 m = __ldg(mask2 + ax);
-      const uint32_t s = tw >> AXC_TARGET_SEG_SHIFT;
-      const uint32_t shv = min(s, 31u);
-      const uint32_t bx = (m.x >> shv) & 1u, by = (m.y >> shv) & 1u;
-      bool hit = (bx | by) != 0u;
-      if (hit && (s >= 31u || !exact)) hit = hit_exact(heads, A, ax, s, prop);
-      if (hit) {
-        i_in = wadd(i_in, w);
-        hitb |= b;
+    }
+    if (!LIT || __any_sync(kFull, need)) {
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        if (!((need >> t) & 1u)) continue;
+        const uint32_t tw = t ? T[3].y : T[3].x;
+        const uint32_t b = 1u << (12 + t);
+        const int32_t w = (int32_t)half_of(W[3], t);
+        const uint32_t s = tw >> AXC_TARGET_SEG_SHIFT;
+        const uint32_t shv = min(s, 31u);
+        const uint32_t bx = (m[t].x >> shv) & 1u, by = (m[t].y >> shv) & 1u;
+        bool hit = (bx | by) != 0u;
+        if (hit && (s >= 31u || !exact)) hit = hit_exact(heads, A, (tw & AXC_TARGET_AXON_MASK) - 1u, s, prop);
+        if (hit) {
+          i_in = wadd(i_in, w);
+          hitb |= b;
+        }
+        const bool fast = gfast && s < 31u && !(m[t].y >> 31) && (bx || by == (s == 0u));
+        slowb |= fast ? 0u : b;
       }
-      const bool fast = gfast && s < 31u && !(m.y >> 31) && (bx || by == (s == 0u));
-      slowb |= fast ? 0u : b;
     }
   }
   hitb_out = hitb;
