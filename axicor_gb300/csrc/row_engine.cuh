@@ -44,6 +44,11 @@ constexpr uint32_t kRowStride = AXC_MAX_DENDRITES;   // slots per neuron row
 constexpr uint32_t kInf = 0xFFFFFFFFu;
 constexpr uint32_t kRowBad = 0x8000u;    // cnt flag: the row holds an invalid target
 
+// Bytes of the fully-lit bitmap of A axons as staged in shared memory (one
+// bit per axon and a spare word, rounded up to the bulk copy's 16 bytes; the
+// global bitmap is allocated at least this large).
+__host__ __device__ __forceinline__ uint32_t lit_smem_bytes(uint32_t A) { return (((A >> 5) + 1) * 4 + 15) & ~15u; }
+
 // physics.cu:322-371 for one slot given the minimum in-tail distance md.
 __device__ __forceinline__ int16_t gsop_weight(int16_t w16, uint32_t md, const VariantParameters& p, int32_t bm,
                                                int32_t raw_pot, int32_t final_dep) {
@@ -649,6 +654,37 @@ __device__ __forceinline__ void row_load(uint4 (&T)[4], uint2 (&W)[4], const uin
   }
 }
 
+// Bulk copy global -> shared completed on an mbarrier (cp.async.bulk, the
+// untiled TMA path: 16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for phase `parity` of bar at most kWaitLimit tries; false: gave up.
+constexpr uint32_t kWaitLimit = 1u << 16;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kWaitLimit; it++)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+
 // The dendrite pass over the slots one lane holds (row_shape) of a row with c
 // used slots: returns the lane's share of the input current and sets, per slot
 // (bit 4j+i; single-slot round t: bit 12+t), hitb = the segment is hit and
@@ -658,8 +694,9 @@ __device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&
                                              RowShape sh, const uint2* __restrict__ mask2, const uint32_t* s_lit,
                                              uint32_t seg_hi, bool exact, bool gfast, uint32_t prop,
                                              const BurstHeads8* heads, uint32_t A, uint32_t& hitb_out,
-                                             uint32_t& slowb_out) {
+                                             uint32_t& slowb_out, bool lit_on = true) {
   int32_t i_in = 0;
+  const bool glit = LIT && lit_on && gfast;   // the fully-lit shortcut applies
   uint32_t hitb = 0, slowb = 0;   // bit 4j+i
 #pragma unroll
   for (int j = 0; j < 4; j++) {
@@ -671,7 +708,7 @@ __device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&
     for (int i = 0; i < 4; i++) {
       const uint32_t t = word_of(T[j], i);
       const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A
-      lit[i] = LIT && gfast && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
+      lit[i] = glit && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
       m[i] = (q0 + i < c && !lit[i]) ? __ldg(mask2 + ax) : make_uint2(0, 0);
     }
     uint32_t need = 0;   // live slots off the fully-lit path
@@ -718,7 +755,7 @@ __device__ __forceinline__ int32_t row_slots(const uint4 (&T)[4], const uint2 (&
       if ((uint32_t)t >= sh.TR || q >= c) continue;
       const uint32_t tw = t ? T[3].y : T[3].x;
       const uint32_t ax = (tw & AXC_TARGET_AXON_MASK) - 1u;
-      if (LIT && gfast && ((tw >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u)) {
+      if (glit && ((tw >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u)) {
         i_in = wadd(i_in, (int32_t)half_of(W[3], t));
         hitb |= 1u << (12 + t);
       } else {
@@ -889,15 +926,15 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
-  extern __shared__ uint32_t s_lit[];
+  __shared__ uint64_t s_bar;
+  extern __shared__ __align__(128) uint32_t s_lit[];
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
+  if (LIT && threadIdx.x == 0) mbar_init(&s_bar, 1);
   lut_to_smem(lut);
   if (threadIdx.x == 0) s_pmax = lut_pmax();
-  if (LIT) {
-    const uint32_t words = (A >> 5) + 1;
-    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) s_lit[w] = __ldg(lit_bits + w);
-  }
   __syncthreads();
+  // the fully-lit bitmap: one bulk copy into shared memory
+  if (LIT && threadIdx.x == 0) bulk_to_smem(s_lit, lit_bits, lit_smem_bytes(A), &s_bar);
   const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
   if (INLINE) {
     build_gtab(gtab, lut, dopamine);
@@ -916,6 +953,11 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   const uint32_t beg = min(wid * per_warp, ecount), end = min(beg + per_warp, ecount);
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
   uint32_t wc = 0, wd = 0;   // spikers this warp listed for the GSOP passes
+  bool lit_on = true;
+  if (LIT) {
+    lit_on = mbar_wait_bounded(&s_bar, 0);
+    if (!lit_on) err |= AXC_ERR_WAIT_LIMIT;   // then without the shortcut (results exact)
+  }
   for (uint32_t base = beg; base < end; base += 32) {
     const uint32_t mine = (base + lane < end) ? __ldg(eval + base + lane) : 0u;
     for (uint32_t sub = 0; sub < 32 && base + sub < end; sub += 4) {
@@ -941,7 +983,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
       uint32_t hitb, slowb;
       int32_t i_in = row_slots<LIT>(T, W, c, g8, sh, mask2, s_lit, seg_hi, exact, gfast, prop, P.axon_heads, A,
-                                    hitb, slowb);
+                                    hitb, slowb, lit_on);
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
@@ -994,6 +1036,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
     wcnt[wid] = wc;
     wcnt[kMaxUpdateWarps + wid] = wd;
   }
+  // a warp that gave up: the copy must land before the block exits
+  if (LIT && !lit_on && !mbar_wait_bounded(&s_bar, 0)) err |= AXC_ERR_WAIT_LIMIT;
   const uint32_t err_any = __reduce_or_sync(kFull, err);
   if (err_any && lane == 0) atomicOr(&ctl->err, err_any);
   block_count(ev_slots, hits, nspk, &ctl->ctr[1]);
@@ -1327,7 +1371,7 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_mult = off; off = al(off + (size_t)A * 4);
   const size_t o_eval = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_fix = off; off = al(off + (with_fix ? (size_t)kFixCap * 4 : 0));
-  const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4);
+  const size_t o_lit = off; off = al(off + ((size_t)std::max(A, N) / 32 + 2) * 4 + 16);
   const size_t o_gsn = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_gdn = off; off = al(off + (size_t)N * 4 + 4);
   const size_t o_am = off; off = al(off + (size_t)N * 16 + 16);
@@ -1409,7 +1453,7 @@ static size_t lit_smem_limit() {
 // The update pass (with the fully-lit bitmap in shared memory when it fits).
 // lc: the learned engine's control block (the pass returns at once on its
 // sparse ticks), or null.
-static bool rows_lit(uint32_t A) { return ((size_t)(A >> 5) + 1) * 4 <= lit_smem_limit(); }
+static bool rows_lit(uint32_t A) { return (size_t)lit_smem_bytes(A) <= lit_smem_limit(); }
 
 // inline: GSOP inside the pass (rows with their movable slots first), else
 // the spikers are listed for launch_rows_gsop.
@@ -1419,7 +1463,7 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
   RowCache& r = *s.rows;
   const int sms = sm_count();
   if (rows_lit(A))
-    k_rows_update<true, INLINE><<<sms, 1024, ((size_t)(A >> 5) + 1) * 4, stream>>>(
+    k_rows_update<true, INLINE><<<sms, 1024, lit_smem_bytes(A), stream>>>(
         v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
         r.lfz, r.wcnt);
   else

@@ -225,6 +225,8 @@ int32_t cu_dma_d2h_io(uint8_t* h_output_history, const uint8_t* d_output_history
 #define AXC_ERR_SOMA_AXON      0x2u /* soma_to_axon >= total_axons (and not 0xFFFFFFFF)  */
 #define AXC_ERR_VIRTUAL_RANGE  0x4u /* virtual_offset + num_virtual_axons > total_axons   */
 #define AXC_ERR_READOUT_RANGE  0x8u /* mapped_soma_id >= padded_n (and not 0xFFFFFFFF)   */
+#define AXC_ERR_WAIT_LIMIT     0x10u /* a bounded on-device wait gave up; the kernel took
+                                        its path without the staged data (results exact) */
 
 /* Library version string. */
 const char* axc_version(void);
