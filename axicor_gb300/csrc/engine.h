@@ -20,7 +20,7 @@ struct ShardCtl {
   uint32_t row_smax;      // row engine: longest row (slots before the first empty) of the batch
   uint32_t seg_max;       // row engine: largest segment of a live slot in the batch
   unsigned long long row_sum;  // row engine: checksum of the batch's targets (slot order)
-  uint32_t gsop_count;    // row engine: spikers listed for the GSOP pass of the tick
+  uint32_t pmax;          // row engine: largest signal_propagation_length of the LUT (batch start)
   uint32_t pad2;
   unsigned long long ctr[8];  // statistics, see axc_shard_counters
 };

@@ -372,6 +372,7 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
     ctl->row_smax = 0;
     ctl->seg_max = 0;
     ctl->row_sum = 0;
+    ctl->pmax = lut_pmax();
   }
   if (n >= N) return;
   const uint32_t a = s2a[n];
@@ -1357,6 +1358,133 @@ __global__ void k_rows_reset_lists(ShardCtl* ctl) {
   ctl->fix_overflow = 0;
 }
 
+// ---------------------------------------------------------------------------
+// per tick 1/4 of the plain engine: the work of k_rows_prologue<false> with
+// ITEMS axons and neurons per thread (items i0 + 256 r).  No barrier before
+// the loads: every thread reads the batch constants (seg_max, the LUT's
+// largest length, set at batch start) itself, next to its own loads.  The
+// evaluated neurons are appended with one atomic per block.
+// ---------------------------------------------------------------------------
+// push_n for the common counts 0 and 1 without the general shift network
+__device__ __forceinline__ void push_few(uint32_t h[8], uint32_t c) {
+  if (c == 1u) {
+#pragma unroll
+    for (int q = 7; q > 0; q--) h[q] = h[q - 1];
+    h[0] = 0u;
+  } else if (c > 1u) {
+    push_n(h, c);
+  }
+}
+
+template <int ITEMS>
+__global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __restrict__ heads, uint32_t A,
+                                                             uint32_t v_seg, const uint32_t* __restrict__ bitmask,
+                                                             uint32_t voff, uint32_t nv,
+                                                             uint32_t* __restrict__ incoming,
+                                                             const uint32_t* __restrict__ batch_counts, uint32_t k,
+                                                             uint2* __restrict__ mask2,
+                                                             const uint32_t* __restrict__ mult,
+                                                             uint8_t* __restrict__ flags,
+                                                             uint8_t* __restrict__ timers, uint32_t N,
+                                                             uint32_t* __restrict__ eval, ShardCtl* __restrict__ ctl,
+                                                             uint32_t raise_err, uint32_t* __restrict__ lit_bits,
+                                                             uint32_t* __restrict__ pend_apply) {
+  __shared__ uint32_t s_base;
+  __shared__ uint32_t s_warp[ITEMS][8];
+  const uint32_t i0 = blockIdx.x * (256u * ITEMS) + threadIdx.x;
+  // all loads first: heads, owners, pending pushes, input bits, timers, constants
+  uint4 hx[ITEMS], hy[ITEMS];
+  uint32_t own[ITEMS], npush[ITEMS];
+  uint8_t tm[ITEMS];
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    const uint32_t i = i0 + 256u * r;
+    npush[r] = 0;
+    own[r] = 0;
+    tm[r] = 0;
+    if (i < A) {
+      const uint4* p = reinterpret_cast<const uint4*>(heads + i);
+      hx[r] = p[0];
+      hy[r] = p[1];
+      own[r] = __ldg(mult + i);
+      if (pend_apply) npush[r] = pend_apply[i];   // the previous tick's soma pushes
+      if (bitmask) {
+        const uint32_t v = i - voff;
+        if (v < nv) npush[r] += (__ldg(bitmask + (v >> 5)) >> (v & 31u)) & 1u;
+      }
+    }
+    if (i < N) tm[r] = timers[i];
+  }
+  const uint32_t seg_max = ctl->seg_max, pmax = ctl->pmax;
+  const bool inc = batch_counts && batch_counts[k] > 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->ctr[0] += 1;
+    if (raise_err) atomicOr(&ctl->err, raise_err);
+    ctl->fix_count = 0;      // the previous tick's fix-up is done
+    ctl->fix_overflow = 0;
+  }
+  const uint32_t hi = min(seg_max, 30u);   // segments 1..hi are the ones the batch's slots use
+  const uint32_t need = hi ? (((2u << hi) - 1u) & ~1u) : 0xFFFFFFFFu;
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t evb[ITEMS];
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++) {
+    const uint32_t i = i0 + 256u * r;
+    bool lit = false;
+    if (i < A) {
+      uint32_t c = npush[r];
+      if (pend_apply && c) pend_apply[i] = 0;
+      if (inc) {
+        const uint32_t ci = incoming[i];
+        if (ci) { c += ci; incoming[i] = 0; }
+      }
+      uint32_t h[8] = {hx[r].x, hx[r].y, hx[r].z, hx[r].w, hy[r].x, hy[r].y, hy[r].z, hy[r].w};
+      push_few(h, c);
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        if (h[j] != AXC_AXON_SENTINEL) h[j] += v_seg;
+      uint4* p = reinterpret_cast<uint4*>(heads + i);
+      p[0] = make_uint4(h[0], h[1], h[2], h[3]);
+      p[1] = make_uint4(h[4], h[5], h[6], h[7]);
+      const uint2 m = split_masks(h, pmax, own[r]);
+      mask2[i] = m;
+      // fully lit: heads 0..6 hit every segment 1..seg_max the batch uses and at
+      // most one soma owns the axon (for those segments the hit is 1 and one
+      // push cannot change it)
+      lit = (m.x & need) == need && !(m.y >> 31);
+    }
+    const uint32_t lb = __ballot_sync(kFull, lit);
+    if (lane == 0 && i < A) lit_bits[i >> 5] = lb;
+    bool ev = false;
+    if (i < N) {
+      if (tm[r] > 0) {                              // physics.cu:168-174 after the burst reset
+        timers[i] = (uint8_t)(tm[r] - 1);
+        flags[i] = flags[i] & 0xF0;
+      } else {
+        ev = true;
+      }
+    }
+    evb[r] = __ballot_sync(kFull, ev);
+    if (lane == 0) s_warp[r][w] = __popc(evb[r]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int q = 0; q < ITEMS * 8; q++) {
+      const uint32_t c = (&s_warp[0][0])[q];
+      (&s_warp[0][0])[q] = tot;
+      tot += c;
+    }
+    s_base = tot ? atomicAdd(&ctl->eval_count[k & 1], tot) : 0u;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < ITEMS; r++)
+    if ((evb[r] >> lane) & 1u)
+      eval[s_base + s_warp[r][w] + __popc(evb[r] & ((1u << lane) - 1u))] = i0 + 256u * r;
+}
+constexpr int kProItems = 1;   // items per thread of k_rows_prologue_plain
+
 }  // namespace
 
 cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
@@ -1503,10 +1631,10 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   if (bitmask && ((uint64_t)a.virtual_offset + a.num_virtual > A)) raise |= AXC_ERR_VIRTUAL_RANGE;
   const uint32_t G = max(A, N);
   if (G)
-    k_rows_prologue<false><<<(G + 255) / 256, 256, 0, stream>>>(
+    k_rows_prologue_plain<kProItems><<<(G + 256 * kProItems - 1) / (256 * kProItems), 256, 0, stream>>>(
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
         have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
-        raise, r.lit, LearnDev{}, a.k > 0 ? s.pend : nullptr);
+        raise, r.lit, a.k > 0 ? s.pend : nullptr);
   if (ev) cudaEventRecord(ev[2], stream);
   // stages: ev[2]..ev[3] the update pass with GSOP, ev[3]..ev[4] fix-up and push
   launch_rows_update<true>(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream);
