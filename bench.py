@@ -139,7 +139,7 @@ class Clocks:
 
 # DRAM traffic per launch of the dominant kernel from one ncu capture of the same kernel on the same
 # workload in its steady state (profiles/k_rows_update_plain-1.5M.md)
-TRAFFIC = {("plain-1.5M", "k_rows_update"): 336.9e6}
+TRAFFIC = {("plain-1.5M", "k_rows_update"): 337.3e6}
 
 
 def workload(name: str):
@@ -170,8 +170,9 @@ def update_kernel_bytes(ticks, evaluated, spikes, N):
 def rows_update_kernel_bytes(evaluated_slots, evaluated_neurons, spikes):
     """Algorithmic bytes of the row engine's update pass (k_rows_update): 6 B per evaluated slot (u32 target +
     i16 weight read), 24 B per evaluated neuron (flags, slot count, list entry, voltage and threshold read;
-    voltage, flags, threshold, timer written), 4 B per spike (soma_to_axon).  The weights GSOP changes are
-    written by the GSOP passes."""
+    voltage, flags, threshold, timer written), 4 B per spike (soma_to_axon).  The pass also applies GSOP to the
+    spikers' movable slots, whose weights it already holds; their write-back (a few hundred kB per tick in the
+    steady state) is not counted."""
     return 6 * evaluated_slots + 24 * evaluated_neurons + 4 * spikes
 
 
@@ -280,8 +281,8 @@ def run_gb300(args, dist: Dist) -> dict | None:
     stage_ms = list(out_ms)
     if engine == 1:
         names = ["network_ids", "prologue", "update", "gsop_fixup_push", "unused"]
-        kernels = {"prologue": "k_rows_prologue", "update": "k_rows_update",
-                   "gsop_fixup_push": "k_rows_gsop+k_rows_gsop_rows+k_rows_fixup+k_rows_push"}
+        kernels = {"prologue": "k_rows_prologue_plain", "update": "k_rows_update",
+                   "gsop_fixup_push": "k_rows_fixup+k_rows_push"}
     else:
         names = ["network_ids", "axons", "update", "push", "gsop"]
         kernels = {"axons": "k_axons", "update": "k_update", "push": "k_push", "gsop": "k_gsop"}
@@ -315,7 +316,9 @@ def run_gb300(args, dist: Dist) -> dict | None:
         "clocks": clk,
         "h2d": B * words * 4,
         "d2h": B * n_out,
-        "launches": K * ((4 * B + 5) if engine == 1 else (4 * B + 2)),
+        # per batch of B ticks: rows: prologue, update, fix-up per tick; push on the last tick;
+        # batch control, burst reset, list reset, owner counts, row copy, write-back
+        "launches": K * ((3 * B + 7) if engine == 1 else (4 * B + 2)),
         "roofline": {"bound": "hbm", "kernel": kernels.get(names[top], names[top]),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": TRAFFIC.get((args.workload, kernels.get(names[top], names[top]))),
