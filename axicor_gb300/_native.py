@@ -24,6 +24,7 @@ ERR_TARGET_RANGE = 0x1
 ERR_SOMA_AXON = 0x2
 ERR_VIRTUAL_RANGE = 0x4
 ERR_READOUT_RANGE = 0x8
+ERR_WAIT_LIMIT = 0x10   # a bounded on-device wait gave up (the kernel took its path without the staged data)
 
 # VariantParameters, genesis-core/src/layout.rs:12-48 (64 bytes)
 VARIANT_DTYPE = np.dtype(
