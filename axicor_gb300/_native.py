@@ -90,6 +90,7 @@ class AxcPopBrainDesc(C.Structure):
         ("virtual_offset", C.c_uint32), ("num_virtual", C.c_uint32),
         ("d_input_bitmask", C.c_void_p), ("words_per_tick", C.c_uint32), ("v_seg", C.c_uint32),
         ("d_lut", C.c_void_p), ("dopamine", C.c_int32), ("tick_base", C.c_uint32),
+        ("bitmask_ticks", C.c_uint32),
     ]
 
 

@@ -8,12 +8,14 @@
 //   k_pop_chunks    one block: cuts every brain's list of evaluated neurons into
 //                   chunks of `chunk` neurons (the work list of the next stages)
 //   k_pop_update    persistent grid over chunks; a block stages the chunk's brain
-//                   descriptor, LUT and GSOP table in shared memory, then runs the
-//                   row engine's update+GSOP with LANES lanes per neuron
+//                   descriptor, LUT, GSOP table and fully-lit bitmap in shared
+//                   memory, then runs the row engine's update with GSOP of the
+//                   movable slots, LANES lanes per neuron
 //   k_pop_fixup     deferred GSOP slots of all brains
 //   k_pop_push      the spikers' own-axon pushes, per chunk
 // Batch prologue/epilogue (once per run): GSOP tables, soma multiplicity,
-// neuron-major rows, weight write-back, each as one launch over all brains.
+// neuron-major rows with their movable slots first, weight write-back, each
+// as one launch over all brains.
 // Every brain evolves exactly as it would alone in axc_step_day_phase_batch.
 
 namespace axc {
@@ -31,6 +33,10 @@ struct PopBrain {
   uint32_t* eval;
   uint32_t* pend;
   ShardCtl* ctl;
+  uint32_t* lit;       // [A/32+1] the tick's fully-lit axons, one bit each
+  uint8_t* lfz;        // [N] movable slots of each row (placed first by the row copy)
+  uint4* amask;        // [N] their row positions
+  uint4* omask;        // [N] the columnar slots placed first (for the write-back)
   uint32_t N, A, voff, nv, words, v_seg, tick_base, pmax;
   int32_t dopamine;
   uint32_t pad[3];
@@ -47,6 +53,7 @@ struct PopCtl {
 namespace {
 
 constexpr uint32_t kPopChunk = 256;   // evaluated neurons per chunk
+constexpr uint32_t kPopLitWords = 12288;   // 48 KB: brains of up to 393k axons stage their fully-lit bitmap
 
 __device__ __forceinline__ uint32_t pmax_of(const VariantParameters* lut) {
   uint32_t m = 0;
@@ -67,6 +74,7 @@ __global__ void __launch_bounds__(256) k_pop_begin(PopBrain* __restrict__ brains
   if (threadIdx.x == 0) {
     b.pmax = pmax_of(b.lut);
     b.ctl->row_smax = 0;
+    b.ctl->seg_max = 0;
     b.ctl->eval_count[0] = 0;
     b.ctl->eval_count[1] = 0;
     b.mask2[b.A] = make_uint2(0u, 0x80000000u);
@@ -90,8 +98,9 @@ __global__ void __launch_bounds__(256) k_pop_mult(const PopBrain* __restrict__ b
   if (a < b.A) atomicAdd(&b.mult[a], 1u);
 }
 
-// columnar -> rows for 32 neurons of one brain, and the batch's burst reset
-// (genesis-compute/src/compute/shard.rs:71, physics.cu:25-30).
+// columnar -> rows for 32 neurons of one brain (build_row: movable slots
+// first), and the batch's burst reset (genesis-compute/src/compute/shard.rs:71,
+// physics.cu:25-30).
 __global__ void __launch_bounds__(256) k_pop_build(const PopBrain* __restrict__ brains,
                                                    const uint32_t* __restrict__ map,
                                                    const uint32_t* __restrict__ first) {
@@ -124,25 +133,26 @@ __global__ void __launch_bounds__(256) k_pop_build(const PopBrain* __restrict__ 
     if (__syncthreads_and(mine)) break;
   }
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ uint32_t s_bc[8], s_bs[8];
+  uint32_t wc = 0, ws = 0;
   for (uint32_t j = warp; j < 32; j += 8) {
     const uint32_t n = n0 + j;
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
-    bool bad = false;
-    for (uint32_t q = lane; q < c; q += 32) {
-      uint32_t t = s_t[q][j];
-      if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
-        t = (t & ~AXC_TARGET_AXON_MASK) | (A + 1u);
-        bad = true;
-      }
-      b.rt[(size_t)n * kRowStride + q] = t;
-      b.rw[(size_t)n * kRowStride + q] = s_w[q][j];
+    const RowBuilt rb = build_row(s_t, s_w, j, n, c, frozen_from(b.lut[b.P.soma_flags[n] >> 4]), A, false, true,
+                                  b.rt, b.rw, b.cnt, b.amask, b.omask, b.lfz);
+    if (lane == 0 && c) {
+      wc = max(wc, c);
+      ws = max(ws, rb.smx);
     }
-    bad = __any_sync(kFull, bad);
-    if (lane == 0) {
-      b.cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
-      if (c) atomicMax(&b.ctl->row_smax, c);
-    }
+  }
+  if (lane == 0) { s_bc[warp] = wc; s_bs[warp] = ws; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t bc = 0, bs = 0;
+    for (int q = 0; q < 8; q++) { bc = max(bc, s_bc[q]); bs = max(bs, s_bs[q]); }
+    if (bc) atomicMax(&b.ctl->row_smax, bc);
+    if (bs) atomicMax(&b.ctl->seg_max, bs);
   }
 }
 
@@ -153,23 +163,11 @@ __global__ void __launch_bounds__(256) k_pop_writeback(const PopBrain* __restric
   __shared__ uint32_t s_c[32];
   uint32_t lb;
   const PopBrain& b = brains[block_brain(map, first, &lb)];
-  const uint32_t N = b.N, n0 = lb * 32;
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t j = warp; j < 32; j += 8) {
-    const uint32_t n = n0 + j;
-    const uint32_t c = n < N ? (b.cnt[n] & 0xFFu) : 0u;
-    if (lane == 0) s_c[j] = c;
-    for (uint32_t q = lane; q < c; q += 32) s_w[q][j] = b.rw[(size_t)n * kRowStride + q];
-  }
-  __syncthreads();
-  uint32_t cmax = 0;
-  for (int j = 0; j < 32; j++) cmax = max(cmax, s_c[j]);
-  const uint32_t c_mine = s_c[lane];
-  for (uint32_t r = warp; r < cmax; r += 8)
-    if (r < c_mine) b.P.dendrite_weights[(size_t)r * N + n0 + lane] = s_w[r][lane];
+  writeback_tile(b.P.dendrite_weights, b.N, lb * 32, b.rw, b.cnt, b.omask, s_w, s_c);
 }
 
-// per tick 1/5: k_rows_prologue per brain (block -> brain map).
+// per tick 1/5: k_rows_prologue per brain (block -> brain map), with the
+// brain's fully-lit bitmap.
 __global__ void __launch_bounds__(256) k_pop_prologue(const PopBrain* __restrict__ brains,
                                                       const uint32_t* __restrict__ map,
                                                       const uint32_t* __restrict__ first,
@@ -182,6 +180,7 @@ __global__ void __launch_bounds__(256) k_pop_prologue(const PopBrain* __restrict
   const uint32_t A = b.A, N = b.N;
   const uint32_t i = lb * 256 + threadIdx.x;
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&const_cast<PopCtl*>(pctl)->ctr[0], 1ull);
+  bool lit = false;
   if (i < A) {
     uint4* p = reinterpret_cast<uint4*>(b.P.axon_heads + i);
     const uint4 x = p[0], y = p[1];
@@ -199,7 +198,17 @@ __global__ void __launch_bounds__(256) k_pop_prologue(const PopBrain* __restrict
       if (h[j] != AXC_AXON_SENTINEL) h[j] += vs;
     p[0] = make_uint4(h[0], h[1], h[2], h[3]);
     p[1] = make_uint4(h[4], h[5], h[6], h[7]);
-    b.mask2[i] = split_masks(h, b.pmax, b.mult[i]);
+    const uint2 m = split_masks(h, b.pmax, b.mult[i]);
+    b.mask2[i] = m;
+    // fully lit: heads 0..6 hit every segment 1..seg_max the brain's slots use
+    // and one soma at most owns the axon (as in k_rows_prologue)
+    const uint32_t hi = min(b.ctl->seg_max, 30u);
+    const uint32_t need = hi ? (((2u << hi) - 1u) & ~1u) : 0xFFFFFFFFu;
+    lit = (m.x & need) == need && !(m.y >> 31);
+  }
+  {
+    const uint32_t lbits = __ballot_sync(kFull, lit);
+    if ((threadIdx.x & 31) == 0 && i < A) b.lit[i >> 5] = lbits;
   }
   bool ev = false;
   if (i < N) {
@@ -256,13 +265,21 @@ struct PopStage {
   uint32_t brain;
 };
 
-__device__ __forceinline__ void stage_brain(PopStage& st, const PopBrain* brains, uint32_t bi) {
+// With lit_cap > 0 the brain's fully-lit bitmap (when it has at most lit_cap
+// words) goes to s_lit too.
+__device__ __forceinline__ void stage_brain(PopStage& st, const PopBrain* brains, uint32_t bi, uint32_t* s_lit,
+                                            uint32_t lit_cap) {
   __syncthreads();
   if (st.brain != bi) {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(brains + bi);
     uint32_t* dst = reinterpret_cast<uint32_t*>(&st.b);
     for (uint32_t i = threadIdx.x; i < sizeof(PopBrain) / 4; i += blockDim.x) dst[i] = src[i];
     __syncthreads();
+    const uint32_t words = (st.b.A >> 5) + 1;
+    if (words <= lit_cap) {
+      const uint32_t* lw = st.b.lit;
+      for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) s_lit[i] = __ldg(lw + i);
+    }
     const uint32_t* ls = reinterpret_cast<const uint32_t*>(st.b.lut);
     uint32_t* ld = reinterpret_cast<uint32_t*>(st.lut);
     for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) ld[i] = ls[i];
@@ -274,11 +291,16 @@ __device__ __forceinline__ void stage_brain(PopStage& st, const PopBrain* brains
 }
 
 // per tick 3/5: update + GSOP of every evaluated neuron of every brain,
-// LANES lanes per neuron (lane g holds slots (4*LANES)*j + 4g .. +3).
+// LANES lanes per neuron (lane g holds slots (4*LANES)*j + 4g .. +3).  Slots
+// of fully-lit axons (the brain's bitmap staged in shared memory when it has
+// at most lit_cap words) hit without a mask gather; a round whose slots are
+// all fully lit skips the mask path warp-uniformly.  GSOP runs over the
+// movable slots only, the first lfz of the row.
 template <int LANES>
 __global__ void __launch_bounds__(256, 3) k_pop_update(const PopBrain* __restrict__ brains, const uint2* __restrict__ chunks,
                                                     PopCtl* __restrict__ pctl, uint2* __restrict__ fix,
-                                                    uint32_t k, uint32_t chunk, uint32_t fix_cap) {
+                                                    uint32_t k, uint32_t chunk, uint32_t fix_cap, uint32_t lit_cap) {
+  extern __shared__ uint32_t s_lit[];
   constexpr int CH = 32 / LANES;      // chunks of 4 slots per lane
   constexpr int G = 32 / LANES;       // neurons per warp
   constexpr int SPAN = 4 * LANES;     // slots covered by one chunk of all lanes
@@ -289,9 +311,11 @@ __global__ void __launch_bounds__(256, 3) k_pop_update(const PopBrain* __restric
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0;
   for (uint32_t ci = blockIdx.x; ci < nch; ci += gridDim.x) {
     const uint2 cd = chunks[ci];
-    stage_brain(st, brains, cd.x);
+    stage_brain(st, brains, cd.x, s_lit, lit_cap);
     const PopBrain& b = st.b;
     const uint32_t A = b.A;
+    const bool use_lit = (A >> 5) + 1 <= lit_cap;
+    const uint32_t seg_hi = min(b.ctl->seg_max, 30u);   // lit bits cover segments 1..seg_hi
     const uint32_t tick = b.tick_base + pctl->tick0 + k;
     const uint32_t ecount = min(b.ctl->eval_count[k & 1] - cd.y, chunk);
     const uint32_t smax = b.ctl->row_smax;
@@ -301,6 +325,7 @@ __global__ void __launch_bounds__(256, 3) k_pop_update(const PopBrain* __restric
       const uint32_t n = valid ? __ldg(b.eval + cd.y + idx) : 0u;
       const uint8_t flags = b.P.soma_flags[n];
       const uint32_t cw = valid ? b.cnt[n] : 0u;
+      const uint32_t lf = valid ? b.lfz[n] : 0u;
       const int32_t thr0 = b.P.threshold_offset[n];
       const int32_t v0 = b.P.soma_voltage[n];
       const uint32_t* trow = b.rt + (size_t)n * kRowStride + 4u * gl;
@@ -326,18 +351,34 @@ __global__ void __launch_bounds__(256, 3) k_pop_update(const PopBrain* __restric
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
       int32_t i_in = 0;
       uint32_t hitb = 0, slowb = 0;
+      const bool glit = use_lit && gfast;
 #pragma unroll
       for (int j = 0; j < CH; j++) {
         const uint32_t q0 = (uint32_t)(SPAN * j) + 4u * gl;
         uint2 m[4];
+        bool lit[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          const uint32_t ax = (word_of(T[j], i) & AXC_TARGET_AXON_MASK) - 1u;
-          m[i] = (q0 + i < c) ? __ldg(b.mask2 + ax) : make_uint2(0, 0);
+          const uint32_t t = word_of(T[j], i);
+          const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;
+          lit[i] = glit && ((t >> AXC_TARGET_SEG_SHIFT) - 1u) < seg_hi && ((s_lit[ax >> 5] >> (ax & 31u)) & 1u);
+          m[i] = (q0 + i < c && !lit[i]) ? __ldg(b.mask2 + ax) : make_uint2(0, 0);
         }
+        uint32_t need = 0;   // live slots off the fully-lit path
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           if (q0 + i >= c) continue;
+          if (lit[i]) {   // segment 1..30 of a fully lit axon: hit, fast GSOP
+            i_in = wadd(i_in, (int32_t)half_of(W[j], i));
+            hitb |= 1u << (4 * j + i);
+          } else {
+            need |= 1u << i;
+          }
+        }
+        if (!__any_sync(kFull, need)) continue;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          if (!((need >> i) & 1u)) continue;
           const uint32_t t = word_of(T[j], i);
           const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
           const uint32_t sh = min(s, 31u);
@@ -395,16 +436,19 @@ __global__ void __launch_bounds__(256, 3) k_pop_update(const PopBrain* __restric
           }
         }
       }
+      // GSOP of the movable slots, the first lf of the row; the frozen ones
+      // (GSOP leaves them as they are) are counted
+      if (spike && gl == 0) gdone += c - lf;
       if (spike) {
 #pragma unroll
         for (int j = 0; j < CH; j++) {
           const uint32_t q0 = (uint32_t)(SPAN * j) + 4u * gl;
-          if (q0 >= c) continue;
+          if (q0 >= lf) continue;
           uint2 wj = W[j];
 #pragma unroll
           for (int i = 0; i < 4; i++) {
             const uint32_t bit = 1u << (4 * j + i);
-            if (q0 + i >= c) continue;
+            if (q0 + i >= lf) continue;
             const int16_t w16 = half_of(wj, i);
             if (!(slowb & bit)) {
               const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
@@ -562,9 +606,18 @@ struct Population {
   PopCtl* d_ctl = nullptr;
   AxcPopSchedule sched{8, 4, 2};
   uint32_t chunk = kPopChunk;
+  uint32_t lit_cap = 0;   // words of the largest fully-lit bitmap the update stages (<= kPopLitWords)
+  std::vector<uint32_t> bm_ticks;   // per brain: bitmask rows (UINT32_MAX without a bitmask)
   std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t>, cudaGraphExec_t> graphs;
   cudaStream_t capture = nullptr;
 };
+
+// Every brain's bitmask holds rows tick0 .. tick0 + ticks - 1.
+static bool pop_ticks_ok(const Population& P, uint32_t tick0, uint64_t ticks) {
+  for (uint32_t b : P.bm_ticks)
+    if ((uint64_t)tick0 + ticks > b) return false;
+  return true;
+}
 
 static cudaError_t pop_upload_map(const std::vector<uint32_t>& v, uint32_t** out) {
   cudaError_t e = cudaMalloc(out, std::max<size_t>(v.size(), 1) * 4);
@@ -579,10 +632,13 @@ static cudaError_t pop_tick(Population& P, uint32_t k, const AxcPopSchedule& sc,
   const uint32_t ub = std::max<uint32_t>(1, sc.update_blocks_per_sm) * sms;
   const uint32_t ab = std::max<uint32_t>(1, sc.aux_blocks_per_sm) * sms;
   const uint32_t cap = std::min(g_pop_fix_cap(), kFixCap);
+  const size_t lit_bytes = (size_t)P.lit_cap * 4;
   if (sc.lanes_per_neuron == 16)
-    k_pop_update<16><<<ub, 256, 0, st>>>(P.d_brains, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk, cap);
+    k_pop_update<16><<<ub, 256, lit_bytes, st>>>(P.d_brains, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk, cap,
+                                                 P.lit_cap);
   else
-    k_pop_update<8><<<ub, 256, 0, st>>>(P.d_brains, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk, cap);
+    k_pop_update<8><<<ub, 256, lit_bytes, st>>>(P.d_brains, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk, cap,
+                                                P.lit_cap);
   k_pop_fixup<<<ab, 256, 0, st>>>(P.d_brains, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk);
   k_pop_push<<<ab, 256, 0, st>>>(P.d_brains, P.count, P.d_chunks, P.d_ctl, k, P.chunk);
   return cudaGetLastError();
@@ -622,6 +678,7 @@ int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, voi
   Population* P = new Population();
   P->count = count;
   P->hb.resize(count);
+  P->bm_ticks.resize(count);
   cudaError_t e = cudaMalloc(&P->d_gtab, (size_t)count * 256 * sizeof(int2));
   std::vector<uint32_t> map_pro, first_pro(count), map_tile, first_tile(count), map_n, first_n(count);
   size_t max_chunks = count;
@@ -645,6 +702,11 @@ int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, voi
     h.eval = s->rows->eval;
     h.pend = s->pend;
     h.ctl = s->ctl;
+    h.lit = s->rows->lit;
+    h.lfz = s->rows->lfz;
+    h.amask = s->rows->amask;
+    h.omask = s->rows->omask;
+    P->lit_cap = std::max(P->lit_cap, std::min((d.total_axons >> 5) + 1, kPopLitWords));
     h.N = d.padded_n;
     h.A = d.total_axons;
     h.voff = d.virtual_offset;
@@ -653,6 +715,7 @@ int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, voi
     h.v_seg = d.v_seg;
     h.tick_base = d.tick_base;
     h.dopamine = d.dopamine;
+    P->bm_ticks[b] = d.d_input_bitmask ? d.bitmask_ticks : 0xFFFFFFFFu;
     first_pro[b] = (uint32_t)map_pro.size();
     for (uint32_t i = 0; i < (std::max(d.padded_n, d.total_axons) + 255) / 256; i++) map_pro.push_back(b);
     first_tile[b] = (uint32_t)map_tile.size();
@@ -693,7 +756,7 @@ int32_t axc_population_set_schedule(void* handle, const AxcPopSchedule* sc) {
 
 int32_t axc_population_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t tpg, void* stream_v) {
   Population* P = static_cast<Population*>(handle);
-  if (!P || tpg == 0 || ticks % tpg) return (int32_t)cudaErrorInvalidValue;
+  if (!P || tpg == 0 || ticks % tpg || !pop_ticks_ok(*P, tick0, ticks)) return (int32_t)cudaErrorInvalidValue;
   cudaStream_t st = static_cast<cudaStream_t>(stream_v);
   auto key = std::make_tuple(tpg, P->sched.lanes_per_neuron, P->sched.update_blocks_per_sm,
                              P->sched.aux_blocks_per_sm * 1000 + std::min(g_pop_fix_cap(), kFixCap) % 1000);
@@ -733,6 +796,7 @@ int32_t axc_population_tune(void* handle, uint32_t tick0, uint32_t trial_ticks, 
   for (uint32_t lanes : {8u, 16u})
     for (uint32_t ub : {2u, 3u, 4u})
       for (uint32_t ab : {1u, 2u}) cands.push_back(AxcPopSchedule{lanes, ub, ab});
+  if (!pop_ticks_ok(*P, tick0, (uint64_t)trial_ticks * cands.size())) return (int32_t)cudaErrorInvalidValue;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

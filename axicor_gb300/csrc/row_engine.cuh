@@ -235,6 +235,116 @@ __device__ __forceinline__ uint32_t row_pos(uint32_t word, uint32_t lane, uint32
   return ((word >> lane) & 1u) ? below : lf + q - below;
 }
 
+// One neuron's row of the row copy, by one warp, from the columns staged in
+// shared memory (column j, c used slots): invalid targets redirected, movable
+// marks, placement (with permute the movable slots first, then the others,
+// each group in slot order), and the neuron's cnt / amask / omask / lfz.
+// Returns, in every lane, the row's largest segment and (want_sum) its
+// targets checksum.
+struct RowBuilt {
+  uint32_t smx;
+  unsigned long long hsum;
+};
+
+__device__ __forceinline__ RowBuilt build_row(uint32_t (*s_t)[33], const int16_t (*s_w)[34], uint32_t j, uint32_t n,
+                                              uint32_t c, int32_t fz, uint32_t A, bool want_sum, bool permute,
+                                              uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
+                                              uint16_t* __restrict__ cnt, uint4* __restrict__ amask,
+                                              uint4* __restrict__ omask, uint8_t* __restrict__ lfz) {
+  const uint32_t lane = threadIdx.x & 31;
+  bool bad = false;
+  uint32_t smx = 0;
+  unsigned long long hsum = 0;
+  uint32_t mv[4], all[4];   // movable / used slots, by columnar position
+#pragma unroll
+  for (int ch = 0; ch < 4; ch++) {
+    const uint32_t q = 32u * ch + lane;
+    bool mov = false;
+    if (q < c) {
+      uint32_t t = s_t[q][j];
+      // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
+      // which sends the slot down the exact path (hit_exact / gsop_general skip it)
+      if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
+        t = (t & ~AXC_TARGET_AXON_MASK) | (A + 1u);
+        s_t[q][j] = t;
+        bad = true;
+      }
+      smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
+      if (want_sum) hsum += slot_mix(t, n * kRowStride + q);
+      mov = !frozen_weight(s_w[q][j], fz);
+    }
+    mv[ch] = __ballot_sync(kFull, mov);
+    all[ch] = __ballot_sync(kFull, q < c);
+  }
+  bad = __any_sync(kFull, bad);
+  smx = __reduce_max_sync(kFull, smx);
+  if (want_sum) hsum = warp_sum(hsum);
+  if (bad) {
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) mv[ch] = all[ch];
+  }
+  const uint32_t lf = __popc(mv[0]) + __popc(mv[1]) + __popc(mv[2]) + __popc(mv[3]);
+  // placement: the movable slots first (permute), else every used slot (identity)
+  uint32_t o[4];
+#pragma unroll
+  for (int ch = 0; ch < 4; ch++) o[ch] = permute ? mv[ch] : all[ch];
+  const uint32_t olf = permute ? lf : c;
+  uint32_t pre = 0, am[4];
+#pragma unroll
+  for (int ch = 0; ch < 4; ch++) {
+    const uint32_t q = 32u * ch + lane;
+    const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
+    pre += __popc(o[ch]);
+    if (q < c) {
+      rt[(size_t)n * kRowStride + pos] = s_t[q][j];
+      rw[(size_t)n * kRowStride + pos] = s_w[q][j];
+    }
+    // the movable slots by row position: the first lf positions, or mv itself
+    const uint32_t lo = 32u * ch;
+    am[ch] = permute ? (lf >= lo + 32u ? kFull : (lf > lo ? (1u << (lf - lo)) - 1u : 0u)) : mv[ch];
+  }
+  if (lane == 0) {
+    cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
+    amask[n] = make_uint4(am[0], am[1], am[2], am[3]);
+    omask[n] = make_uint4(o[0], o[1], o[2], o[3]);
+    lfz[n] = (uint8_t)lf;
+  }
+  return RowBuilt{smx, hsum};
+}
+
+// Batch end, 32 neurons from n0 by a 256-thread block: weights rows -> columnar
+// for the slots before the first empty target (slot q of neuron n from row
+// position row_pos of its omask).
+__device__ __forceinline__ void writeback_tile(int16_t* __restrict__ weights, uint32_t N, uint32_t n0,
+                                               const int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
+                                               const uint4* __restrict__ omask, int16_t (*s_w)[34],
+                                               uint32_t* s_c) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t j = warp; j < 32; j += 8) {
+    const uint32_t n = n0 + j;
+    const uint32_t c = n < N ? (cnt[n] & 0xFFu) : 0u;
+    if (lane == 0) s_c[j] = c;
+    if (c == 0) continue;
+    const uint4 om = omask[n];
+    const uint32_t o[4] = {om.x, om.y, om.z, om.w};
+    const uint32_t olf = __popc(om.x) + __popc(om.y) + __popc(om.z) + __popc(om.w);
+    uint32_t pre = 0;
+#pragma unroll
+    for (int ch = 0; ch < 4; ch++) {
+      const uint32_t q = 32u * ch + lane;
+      const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
+      pre += __popc(o[ch]);
+      if (q < c) s_w[q][j] = rw[(size_t)n * kRowStride + pos];
+    }
+  }
+  __syncthreads();
+  uint32_t cmax = 0;
+  for (int j = 0; j < 32; j++) cmax = max(cmax, s_c[j]);
+  const uint32_t c_mine = s_c[lane];
+  for (uint32_t r = warp; r < cmax; r += 8)
+    if (r < c_mine) weights[(size_t)r * N + n0 + lane] = s_w[r][lane];
+}
+
 // Batch start: columnar -> rows.  32 neurons per 256-thread block; the
 // columns are read 8 slots at a time until every neuron of the tile has met
 // its first empty target.  A slot whose weight GSOP may still move (not
@@ -287,68 +397,12 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     const uint32_t n = n0 + j;
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
-    const int32_t fz = frozen_from(VARIANT_LUT[flags[n] >> 4]);
-    bool bad = false;
-    uint32_t smx = 0;
-    unsigned long long hsum = 0;
-    uint32_t mv[4], all[4];   // movable / used slots, by columnar position
-#pragma unroll
-    for (int ch = 0; ch < 4; ch++) {
-      const uint32_t q = 32u * ch + lane;
-      bool mov = false;
-      if (q < c) {
-        uint32_t t = s_t[q][j];
-        // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
-        // which sends the slot down the exact path (hit_exact / gsop_general skip it)
-        if ((t & AXC_TARGET_AXON_MASK) - 1u >= A) {
-          t = (t & ~AXC_TARGET_AXON_MASK) | (A + 1u);
-          s_t[q][j] = t;
-          bad = true;
-        }
-        smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
-        if (want_sum) hsum += slot_mix(t, n * kRowStride + q);
-        mov = !frozen_weight(s_w[q][j], fz);
-      }
-      mv[ch] = __ballot_sync(kFull, mov);
-      all[ch] = __ballot_sync(kFull, q < c);
-    }
-    bad = __any_sync(kFull, bad);
-    smx = __reduce_max_sync(kFull, smx);
-    if (want_sum) hsum = warp_sum(hsum);
-    if (bad) {
-#pragma unroll
-      for (int ch = 0; ch < 4; ch++) mv[ch] = all[ch];
-    }
-    const uint32_t lf = __popc(mv[0]) + __popc(mv[1]) + __popc(mv[2]) + __popc(mv[3]);
-    // placement: the movable slots first (permute), else every used slot (identity)
-    uint32_t o[4];
-#pragma unroll
-    for (int ch = 0; ch < 4; ch++) o[ch] = permute ? mv[ch] : all[ch];
-    const uint32_t olf = permute ? lf : c;
-    uint32_t pre = 0, am[4];
-#pragma unroll
-    for (int ch = 0; ch < 4; ch++) {
-      const uint32_t q = 32u * ch + lane;
-      const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
-      pre += __popc(o[ch]);
-      if (q < c) {
-        rt[(size_t)n * kRowStride + pos] = s_t[q][j];
-        rw[(size_t)n * kRowStride + pos] = s_w[q][j];
-      }
-      // the movable slots by row position: the first lf positions, or mv itself
-      const uint32_t lo = 32u * ch;
-      am[ch] = permute ? (lf >= lo + 32u ? kFull : (lf > lo ? (1u << (lf - lo)) - 1u : 0u)) : mv[ch];
-    }
-    if (lane == 0) {
-      cnt[n] = (uint16_t)(c | (bad ? kRowBad : 0u));
-      amask[n] = make_uint4(am[0], am[1], am[2], am[3]);
-      omask[n] = make_uint4(o[0], o[1], o[2], o[3]);
-      lfz[n] = (uint8_t)lf;
-      if (c) {
-        wc = max(wc, c);
-        ws = max(ws, smx);
-        wh += hsum + slot_mix(c, n);
-      }
+    const RowBuilt rb = build_row(s_t, s_w, j, n, c, frozen_from(VARIANT_LUT[flags[n] >> 4]), A, want_sum != 0u,
+                                  permute != 0u, rt, rw, cnt, amask, omask, lfz);
+    if (lane == 0 && c) {
+      wc = max(wc, c);
+      ws = max(ws, rb.smx);
+      wh += rb.hsum + slot_mix(c, n);
     }
   }
   if (lane == 0) { s_bc[warp] = wc; s_bs[warp] = ws; s_bh[warp] = wh; }
@@ -387,31 +441,7 @@ __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ we
                                                         const uint4* __restrict__ omask) {
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_c[32];
-  const uint32_t n0 = blockIdx.x * 32;
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t j = warp; j < 32; j += 8) {
-    const uint32_t n = n0 + j;
-    const uint32_t c = n < N ? (cnt[n] & 0xFFu) : 0u;
-    if (lane == 0) s_c[j] = c;
-    if (c == 0) continue;
-    const uint4 om = omask[n];
-    const uint32_t o[4] = {om.x, om.y, om.z, om.w};
-    const uint32_t olf = __popc(om.x) + __popc(om.y) + __popc(om.z) + __popc(om.w);
-    uint32_t pre = 0;
-#pragma unroll
-    for (int ch = 0; ch < 4; ch++) {
-      const uint32_t q = 32u * ch + lane;
-      const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
-      pre += __popc(o[ch]);
-      if (q < c) s_w[q][j] = rw[(size_t)n * kRowStride + pos];
-    }
-  }
-  __syncthreads();
-  uint32_t cmax = 0;
-  for (int j = 0; j < 32; j++) cmax = max(cmax, s_c[j]);
-  const uint32_t c_mine = s_c[lane];
-  for (uint32_t r = warp; r < cmax; r += 8)
-    if (r < c_mine) weights[(size_t)r * N + n0 + lane] = s_w[r][lane];
+  writeback_tile(weights, N, blockIdx.x * 32, rw, cnt, omask, s_w, s_c);
 }
 
 // Learned engine, in the prologue: per-tile active synapses and heads in

@@ -21,6 +21,7 @@ class Brain:
         self.lay, self.state0, self.heads0 = S.generate_brain(w.spec())
         self.vram = S.VramState(self.lay.padded_n, self.lay.total_axons)
         self.words = max((w.num_inputs + 31) // 32, 1)
+        self.ticks = ticks
         self.bitmask = S.input_bitmask(w.seed, tick_base, ticks, w.num_inputs, w.rate_q32)
         self.d_bitmask = S.device_array(self.bitmask)
         self.d_lut = S.device_array(np.ascontiguousarray(w.lut))
@@ -44,6 +45,7 @@ class Brain:
         d.d_lut = self.d_lut
         d.dopamine = self.w.dopamine
         d.tick_base = self.tick_base
+        d.bitmask_ticks = self.ticks
         return d
 
     @property
@@ -53,6 +55,8 @@ class Brain:
 
     def run_alone(self, tick0: int, ticks: int, batch: int, engine: S.ShardEngine | None = None) -> None:
         """The same ticks through axc_step_day_phase_batch (the process LUT is set to this brain's)."""
+        if tick0 + ticks > self.ticks:
+            raise ValueError(f"ticks {tick0}..{tick0 + ticks} exceed the brain's {self.ticks}-tick input bitmask")
         S.upload_lut(self.w.lut)
         eng = engine or S.ShardEngine(self.vram)
         io = S.IoDeviceBuffers(self.words, 0, 0, batch)

@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--learned-ratio", type=float, default=3.0)
     ap.add_argument("--pop-brains", type=int, default=512)
     ap.add_argument("--pop-ticks", type=int, default=2000)
+    ap.add_argument("--pop-warmup", type=int, default=600)
     ap.add_argument("--ticks-per-step", type=int, default=100)
     ap.add_argument("--outputs", type=int, default=4096)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
@@ -411,8 +412,11 @@ def run_reference(args, dist: Dist) -> None:
 
 def run_population(args) -> None:
     """512 independent brains (neurons log-uniform in [1k,100k], slots in {32,64,96,128}, per-brain
-    threshold / leak shift / GSOP / input rate), 2,000 ticks each: the population engine against the same
-    brains stepped one after another through the batch entry point; every final state compared."""
+    threshold / leak shift / GSOP / input rate), ticks [warm-up, warm-up + 2,000) of each timed: the population
+    engine against the same brains stepped one after another through the batch entry point; every final
+    state compared.  The schedule is tuned on live ticks after the warm-up (the weights' GSOP settles in the
+    first few hundred ticks, and the fastest schedule differs before and after); both arms run the warm-up
+    untimed from the same initial states."""
     import hashlib
     import torch
     import __graft_entry__ as G
@@ -422,10 +426,11 @@ def run_population(args) -> None:
     from axicor_gb300 import workloads as W
     lib = N.lib()
     lib.gpu_set_device(0)
-    count, ticks, tpg = args.pop_brains, args.pop_ticks, args.ticks_per_step
+    count, ticks, tpg, warm = args.pop_brains, args.pop_ticks, args.ticks_per_step, args.pop_warmup
+    assert warm % tpg == 0 and ticks % tpg == 0
     t0 = time.perf_counter()
-    ws = W.population(count=count, ticks=ticks)
-    brains = [Pop.Brain(w, ticks) for w in ws]
+    ws = W.population(count=count, ticks=warm + ticks)
+    brains = [Pop.Brain(w, warm + ticks) for w in ws]
     synapses = sum(b.synapses for b in brains)
     neurons = sum(b.lay.num_neurons for b in brains)
     setup_s = time.perf_counter() - t0
@@ -437,16 +442,21 @@ def run_population(args) -> None:
         return h.hexdigest()
 
     pop = Pop.Population(brains)
-    sc, cand_ms = pop.tune(0, 2, None)
-    pop.run(0, tpg, tpg)                       # captures the graph (untimed)
+    if warm:
+        pop.run(0, warm, tpg)                  # untimed
+    sc, cand_ms = pop.tune(warm, 2, None)      # 12 candidates x 2 live ticks
     for b in brains:
         b.reset()
+    pop.run(0, warm if warm else tpg, tpg)     # the warm-up again with the chosen schedule (captures its graph)
+    if not warm:
+        for b in brains:
+            b.reset()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = Clocks(0)
     clocks.start()
     e0.record()
-    pop.run(0, ticks, tpg)
+    pop.run(warm, ticks, tpg)
     e1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -456,12 +466,14 @@ def run_population(args) -> None:
     pop.close()
     # sequential: each brain alone through the batch entry point (graphs captured untimed first)
     for b in brains:
-        b.run_alone(0, tpg, batch=tpg)
         b.reset()
+        b.run_alone(0, warm if warm else tpg, batch=tpg)   # untimed (captures the graphs)
+        if not warm:
+            b.reset()
     torch.cuda.synchronize()
     s0 = time.perf_counter()
     for b in brains:
-        b.run_alone(0, ticks, batch=tpg)
+        b.run_alone(warm, ticks, batch=tpg)
     torch.cuda.synchronize()
     seq_s = time.perf_counter() - s0
     same = sum(1 for b, d in zip(brains, pop_digest) if digest(b) == d)
@@ -471,7 +483,8 @@ def run_population(args) -> None:
         "warmup": 0, "ms_per_step": pop_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (seeded generator, inputs resident in HBM)",
         "config": {"workload": f"population-{count}", "brains": count, "neurons": neurons, "synapses": synapses,
-                   "ticks": ticks, "ticks_per_graph": tpg,
+                   "ticks": ticks, "timed_ticks": [warm, warm + ticks], "warmup_ticks": warm,
+                   "ticks_per_graph": tpg,
                    "schedule": {"lanes_per_neuron": sc.lanes_per_neuron,
                                 "update_blocks_per_sm": sc.update_blocks_per_sm,
                                 "aux_blocks_per_sm": sc.aux_blocks_per_sm}},

@@ -338,6 +338,8 @@ typedef struct AxcPopBrainDesc {
   const VariantParameters* d_lut;     /* device, 16 entries, this brain's LUT */
   int32_t dopamine;
   uint32_t tick_base;                 /* global tick of bitmask row 0 */
+  uint32_t bitmask_ticks;             /* rows of d_input_bitmask: a run or tuning past them is
+                                         refused with cudaErrorInvalidValue before any launch */
 } AxcPopBrainDesc;
 
 /* Kernel schedule of the population stages (chosen by axc_population_tune). */
@@ -351,7 +353,8 @@ int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, voi
 /* Runs ticks [tick0, tick0 + ticks) of every brain (bitmask row tick0 + t),
  * in graphs of ticks_per_graph ticks (ticks must be a multiple), with the
  * batch prologue/epilogue (row copy, weight write-back) once per call.
- * Asynchronous on `stream`. */
+ * Refused (cudaErrorInvalidValue) when a brain's bitmask has fewer than
+ * tick0 + ticks rows.  Asynchronous on `stream`. */
 int32_t axc_population_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t ticks_per_graph,
                            void* stream);
 /* Times every candidate schedule on `trial_ticks` ticks from the current

@@ -113,3 +113,25 @@ def test_population_fixup_rescan(gpu):
         pop.close()
         for b in brains:
             b.free()
+
+
+def test_population_refuses_ticks_past_the_bitmask(gpu):
+    """A run or a tuning past a brain's input bitmask is refused on the host, before any launch."""
+    ticks = 20
+    ws = mixed_population(count=4, seed=9)
+    brains = [Pop.Brain(w, ticks) for w in ws]
+    pop = Pop.Population(brains)
+    try:
+        with pytest.raises(RuntimeError):
+            pop.run(10, 20, 10)                 # rows 10..29 of a 20-row bitmask
+        with pytest.raises(RuntimeError):
+            pop.tune(0, 2, None)                # 12 candidates x 2 ticks = 24 rows
+        with pytest.raises(ValueError):
+            brains[0].run_alone(10, 20, 10)
+        pop.run(0, ticks, 10)                   # the whole bitmask: accepted
+        N.lib().gpu_device_synchronize()
+        assert pop.counters()[0] == ticks
+    finally:
+        pop.close()
+        for b in brains:
+            b.free()
