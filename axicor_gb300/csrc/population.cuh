@@ -12,7 +12,8 @@
 //                   memory, then runs the row engine's update with GSOP of the
 //                   movable slots, LANES lanes per neuron
 //   k_pop_fixup     deferred GSOP slots of all brains
-//   k_pop_push      the spikers' own-axon pushes, per chunk
+//   k_pop_push      the spikers' own-axon pushes, per chunk, on a graph's last
+//                   tick (on the others the next prologue applies them)
 // Batch prologue/epilogue (once per run): GSOP tables, soma multiplicity,
 // neuron-major rows with their movable slots first, weight write-back, each
 // as one launch over all brains.
@@ -167,11 +168,12 @@ __global__ void __launch_bounds__(256) k_pop_writeback(const PopBrain* __restric
 }
 
 // per tick 1/5: k_rows_prologue per brain (block -> brain map), with the
-// brain's fully-lit bitmap.
+// brain's fully-lit bitmap.  apply_pend: the previous tick's soma pushes,
+// deferred to here within a graph (pushes commute), go in with the input pushes.
 __global__ void __launch_bounds__(256) k_pop_prologue(const PopBrain* __restrict__ brains,
                                                       const uint32_t* __restrict__ map,
                                                       const uint32_t* __restrict__ first,
-                                                      const PopCtl* __restrict__ pctl, uint32_t k) {
+                                                      PopCtl* __restrict__ pctl, uint32_t k, uint32_t apply_pend) {
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[8];
   uint32_t lb;
@@ -179,7 +181,11 @@ __global__ void __launch_bounds__(256) k_pop_prologue(const PopBrain* __restrict
   const PopBrain& b = brains[bi];
   const uint32_t A = b.A, N = b.N;
   const uint32_t i = lb * 256 + threadIdx.x;
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&const_cast<PopCtl*>(pctl)->ctr[0], 1ull);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&pctl->ctr[0], 1ull);
+    pctl->fix_count = 0;      // the previous tick's fix-up is done
+    pctl->fix_overflow = 0;
+  }
   bool lit = false;
   if (i < A) {
     uint4* p = reinterpret_cast<uint4*>(b.P.axon_heads + i);
@@ -190,6 +196,13 @@ __global__ void __launch_bounds__(256) k_pop_prologue(const PopBrain* __restrict
       const uint32_t v = i - b.voff;
       if (v < b.nv)
         npush += (__ldg(b.bitmask + (size_t)(pctl->tick0 + k) * b.words + (v >> 5)) >> (v & 31u)) & 1u;
+    }
+    if (apply_pend) {
+      const uint32_t c = b.pend[i];
+      if (c) {
+        npush += c;
+        b.pend[i] = 0;
+      }
     }
     push_n(h, npush);
     const uint32_t vs = b.v_seg;
@@ -485,14 +498,16 @@ __global__ void __launch_bounds__(256, 3) k_pop_update(const PopBrain* __restric
 }
 
 // per tick 4/5: deferred GSOP slots of all brains.
-__global__ void __launch_bounds__(256) k_pop_fixup(const PopBrain* __restrict__ brains, const uint2* __restrict__ chunks,
-                                                   PopCtl* __restrict__ pctl, const uint2* __restrict__ fix,
-                                                   uint32_t k, uint32_t chunk) {
+__global__ void __launch_bounds__(256) k_pop_fixup(const PopBrain* __restrict__ brains, uint32_t count,
+                                                   const uint2* __restrict__ chunks, PopCtl* __restrict__ pctl,
+                                                   const uint2* __restrict__ fix, uint32_t k, uint32_t chunk) {
   const uint32_t nfix = pctl->fix_count;
   const uint32_t overflow = pctl->fix_overflow;
-  if (nfix == 0 && !overflow) return;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  // the next tick's lists (the slot was last used two ticks ago)
+  for (uint32_t b = tid; b < count; b += stride) brains[b].ctl->eval_count[(k + 1) & 1] = 0;
+  if (nfix == 0 && !overflow) return;
   if (!overflow) {
     for (uint32_t i = tid; i < nfix; i += stride) {
       const PopBrain& b = brains[fix[i].x];
@@ -527,17 +542,13 @@ __global__ void __launch_bounds__(256) k_pop_fixup(const PopBrain* __restrict__ 
   }
 }
 
-// per tick 5/5: pushes, per chunk; the next tick's counters.
+// per tick 5/5, on a graph's last tick only: the spikers' own-axon pushes,
+// per chunk (on the other ticks the next prologue applies them).
 __global__ void __launch_bounds__(256) k_pop_push(const PopBrain* __restrict__ brains, uint32_t count,
                                                   const uint2* __restrict__ chunks, PopCtl* __restrict__ pctl,
                                                   uint32_t k, uint32_t chunk) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t stride = gridDim.x * blockDim.x;
-  if (tid == 0) {
-    pctl->fix_count = 0;
-    pctl->fix_overflow = 0;
-  }
-  for (uint32_t b = tid; b < count; b += stride) brains[b].ctl->eval_count[(k + 1) & 1] = 0;
   const uint32_t nch = pctl->nchunks[k & 1];
   for (uint32_t w = tid; w < nch * chunk; w += stride) {
     const uint2 cd = chunks[w / chunk];
@@ -625,9 +636,12 @@ static cudaError_t pop_upload_map(const std::vector<uint32_t>& v, uint32_t** out
   return e;
 }
 
-static cudaError_t pop_tick(Population& P, uint32_t k, const AxcPopSchedule& sc, cudaStream_t st) {
+// One tick of a graph of `ticks` ticks: the soma pushes of tick k go in with
+// tick k+1's prologue, and the last tick pushes its own.
+static cudaError_t pop_tick(Population& P, uint32_t k, uint32_t ticks, const AxcPopSchedule& sc, cudaStream_t st) {
   const int sms = sm_count();
-  if (P.nblk_pro) k_pop_prologue<<<P.nblk_pro, 256, 0, st>>>(P.d_brains, P.d_map_pro, P.d_first_pro, P.d_ctl, k);
+  if (P.nblk_pro)
+    k_pop_prologue<<<P.nblk_pro, 256, 0, st>>>(P.d_brains, P.d_map_pro, P.d_first_pro, P.d_ctl, k, k > 0 ? 1u : 0u);
   k_pop_chunks<<<1, 1024, 0, st>>>(P.d_brains, P.count, P.d_chunks, P.d_ctl, k, P.chunk);
   const uint32_t ub = std::max<uint32_t>(1, sc.update_blocks_per_sm) * sms;
   const uint32_t ab = std::max<uint32_t>(1, sc.aux_blocks_per_sm) * sms;
@@ -639,8 +653,8 @@ static cudaError_t pop_tick(Population& P, uint32_t k, const AxcPopSchedule& sc,
   else
     k_pop_update<8><<<ub, 256, lit_bytes, st>>>(P.d_brains, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk, cap,
                                                 P.lit_cap);
-  k_pop_fixup<<<ab, 256, 0, st>>>(P.d_brains, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk);
-  k_pop_push<<<ab, 256, 0, st>>>(P.d_brains, P.count, P.d_chunks, P.d_ctl, k, P.chunk);
+  k_pop_fixup<<<ab, 256, 0, st>>>(P.d_brains, P.count, P.d_chunks, P.d_ctl, P.d_fix, k, P.chunk);
+  if (k + 1 == ticks) k_pop_push<<<ab, 256, 0, st>>>(P.d_brains, P.count, P.d_chunks, P.d_ctl, k, P.chunk);
   return cudaGetLastError();
 }
 
@@ -769,7 +783,7 @@ int32_t axc_population_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_
     e = cudaStreamBeginCapture(P->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return (int32_t)e;
     cudaError_t le = cudaSuccess;
-    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = pop_tick(*P, k, P->sched, P->capture);
+    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) le = pop_tick(*P, k, tpg, P->sched, P->capture);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(P->capture, &g);
     if (le != cudaSuccess) e = le;
@@ -806,7 +820,7 @@ int32_t axc_population_tune(void* handle, uint32_t tick0, uint32_t trial_ticks, 
   for (size_t i = 0; i < cands.size() && e == cudaSuccess; i++) {
     k_pop_next_graph<<<(P->count + 255) / 256, 256, 0, st>>>(P->d_brains, P->count, P->d_ctl, tick);
     cudaEventRecord(e0, st);
-    for (uint32_t k = 0; k < trial_ticks && e == cudaSuccess; k++) e = pop_tick(*P, k, cands[i], st);
+    for (uint32_t k = 0; k < trial_ticks && e == cudaSuccess; k++) e = pop_tick(*P, k, trial_ticks, cands[i], st);
     cudaEventRecord(e1, st);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     float ms = 0.f;
