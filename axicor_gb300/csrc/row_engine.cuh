@@ -1013,8 +1013,11 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
       const bool gfast = exact && prop <= 16u;
       if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
       uint32_t hitb, slowb;
-      int32_t i_in = row_slots<LIT>(T, W, c, g8, sh, mask2, s_lit, seg_hi, exact, gfast, prop, P.axon_heads, A,
-                                    hitb, slowb, lit_on);
+      // the fully-lit test reads the bitmap from shared memory (LIT) or, when it
+      // did not fit there, from global memory (1 bit per axon: far fewer bytes
+      // to keep in L1/L2 than the 8-byte masks)
+      int32_t i_in = row_slots<true>(T, W, c, g8, sh, mask2, LIT ? s_lit : lit_bits, seg_hi, exact, gfast, prop,
+                                     P.axon_heads, A, hitb, slowb, lit_on);
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 1));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 2));
       i_in = wadd(i_in, __shfl_xor_sync(kFull, i_in, 4));
