@@ -266,6 +266,46 @@ def test_plain_1_5m_first_ticks(gpu):
         tw.close()
 
 
+def test_plain_1_5m_steady_state_batches(gpu):
+    """The 1.5M-neuron brain at full size in its steady state: 700 ticks through the batch path (by then the
+    weights outside the input axons' slots sit at zero-inertia ranks and nearly every axon is fully lit, so
+    the movable-first rows, the 189 KB shared-memory bitmap and the deferred pushes all carry the tick),
+    then two 10-tick batches on the GPU and on the oracle from the same state, whole state and heads
+    compared after each."""
+    w = W.config1()
+    lay, state, heads = S.generate_brain(w.spec())
+    S.upload_lut(w.lut)
+    vram = S.VramState(lay.padded_n, lay.total_axons)
+    vram.upload_state(state)
+    vram.upload_axon_heads(heads)
+    del state, heads
+    eng = S.ShardEngine(vram)
+    words = (w.num_inputs + 31) // 32
+    warm, batch = 700, 10
+    bm = S.input_bitmask(w.seed, 0, warm + 2 * batch, w.num_inputs, w.rate_q32)
+    io = S.IoDeviceBuffers(words, 0, 0, 100)
+    for t in range(0, warm, 100):
+        eng.step_day_phase_batch(100, io, bm[t * words:(t + 100) * words], None, None, lay.virtual_offset,
+                                 w.num_inputs, None, 1, 0, t)
+    eng.synchronize()
+    h_state, h_heads = vram.download_state(), vram.download_heads()
+    sv = StateView(h_state, lay.padded_n)
+    live = sv.targets != 0
+    frozen = live & (np.abs(sv.weights.astype(np.int32)) >= 2048)
+    assert frozen.sum() > 0.99 * live.sum()
+    io10 = S.IoDeviceBuffers(words, 0, 0, batch)
+    for b in range(2):
+        t0 = warm + b * batch
+        rows = bm[t0 * words:(t0 + batch) * words]
+        eng.step_day_phase_batch(batch, io10, rows, None, None, lay.virtual_offset, w.num_inputs, None, 1, 0, t0)
+        eng.synchronize()
+        oracle.run_ticks(h_state, h_heads, w.lut, lay.padded_n, lay.total_axons, 1, t0, batch, rows, words,
+                         lay.virtual_offset, w.num_inputs)
+        assert np.array_equal(vram.download_heads(), h_heads), f"heads differ after ticks {t0}..{t0 + batch}"
+        assert np.array_equal(vram.download_state(), h_state), f"state differs after ticks {t0}..{t0 + batch}"
+    assert vram.error_flags() == 0
+
+
 def test_legacy_launchers_match_stages(gpu):
     """launch_propagate_axons / launch_update_neurons / launch_apply_gsop / launch_record_readout
     against the oracle's stages (ffi.rs:193-233)."""
