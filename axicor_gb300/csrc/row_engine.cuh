@@ -502,61 +502,66 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err,
                                                        uint32_t* __restrict__ lit_bits, LearnDev L,
                                                        uint32_t* __restrict__ pend_apply) {
-  __shared__ uint32_t s_pmax, s_base, s_need, s_act;
-  __shared__ int s_inc;
+  __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[8];
-  if (threadIdx.x == 0) {
-    s_pmax = lut_pmax();
-    const uint32_t hi = min(ctl->seg_max, 30u);   // segments 1..hi are the ones the batch's slots use
-    s_need = hi ? (((2u << hi) - 1u) & ~1u) : 0xFFFFFFFFu;
-    // segments the batch's slots use: 0..seg_max (bit 31: any segment >= 31)
-    s_act = ctl->seg_max >= 31u ? 0xFFFFFFFFu : ((2u << ctl->seg_max) - 1u);
-    s_inc = batch_counts && batch_counts[k] > 0;
-    if (blockIdx.x == 0) {
-      ctl->ctr[0] += 1;
-      if (raise_err) atomicOr(&ctl->err, raise_err);
-      ctl->fix_count = 0;      // the previous tick's fix-up is done
-      ctl->fix_overflow = 0;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  // every load first, with no barrier before them: heads, owners, pending
+  // pushes, input bit; the batch constants are read by every thread (the LUT's
+  // largest length and the largest segment, both set by the row copy)
+  uint4 hx = make_uint4(0, 0, 0, 0), hy = hx;
+  uint32_t own = 0, pc = 0, ibit = 0;
+  const uint8_t tm = i < N ? timers[i] : (uint8_t)0;
+  if (i < A) {
+    const uint4* p = reinterpret_cast<const uint4*>(heads + i);
+    hx = p[0];
+    hy = p[1];
+    own = __ldg(mult + i);
+    if (pend_apply) pc = pend_apply[i];   // the previous tick's soma pushes (pushes commute)
+    if (bitmask) {
+      const uint32_t v = i - voff;
+      if (v < nv) ibit = (__ldg(bitmask + (v >> 5)) >> (v & 31u)) & 1u;
     }
   }
-  __syncthreads();
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t pmax = ctl->pmax, seg_max = ctl->seg_max;
+  const uint32_t hi = min(seg_max, 30u);   // segments 1..hi are the ones the batch's slots use
+  const uint32_t need = hi ? (((2u << hi) - 1u) & ~1u) : 0xFFFFFFFFu;
+  // segments the batch's slots use: 0..seg_max (bit 31: any segment >= 31)
+  const uint32_t act = seg_max >= 31u ? 0xFFFFFFFFu : ((2u << seg_max) - 1u);
+  const bool inc = batch_counts && batch_counts[k] > 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->ctr[0] += 1;
+    if (raise_err) atomicOr(&ctl->err, raise_err);
+    ctl->fix_count = 0;      // the previous tick's fix-up is done
+    ctl->fix_overflow = 0;
+  }
   bool lit = false;
   uint32_t fan = 0, inflight = 0;   // LEARN: active synapses and heads in flight of axon i
   if (i < A) {
-    uint4* p = reinterpret_cast<uint4*>(heads + i);
-    const uint4 x = p[0], y = p[1];
-    uint32_t h[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
-    uint32_t npush = 0;
-    if (bitmask) {
-      const uint32_t v = i - voff;
-      if (v < nv) npush += (__ldg(bitmask + (v >> 5)) >> (v & 31u)) & 1u;
-    }
-    if (s_inc) {
+    uint32_t h[8] = {hx.x, hx.y, hx.z, hx.w, hy.x, hy.y, hy.z, hy.w};
+    uint32_t npush = ibit + pc;
+    if (pc) pend_apply[i] = 0;
+    if (inc) {
       const uint32_t c = incoming[i];
       if (c) { npush += c; incoming[i] = 0; }
-    }
-    if (pend_apply) {   // the previous tick's soma pushes (pushes commute: each inserts a zero head)
-      const uint32_t c = pend_apply[i];
-      if (c) { npush += c; pend_apply[i] = 0; }
     }
     push_n(h, npush);
 #pragma unroll
     for (int j = 0; j < 8; j++)
       if (h[j] != AXC_AXON_SENTINEL) h[j] += v_seg;
+    uint4* p = reinterpret_cast<uint4*>(heads + i);
     p[0] = make_uint4(h[0], h[1], h[2], h[3]);
     p[1] = make_uint4(h[4], h[5], h[6], h[7]);
-    const uint2 m = split_masks(h, s_pmax, mult[i]);
+    const uint2 m = split_masks(h, pmax, own);
     mask2[i] = m;
     // fully lit: heads 0..6 hit every segment 1..seg_max the batch uses and at
     // most one soma owns the axon, so for those segments the hit is 1 and one
     // push cannot change it
-    lit = (m.x & s_need) == s_need && !(m.y >> 31);
+    lit = (m.x & need) == need && !(m.y >> 31);
     if (LEARN) {
       // active: some head covers a segment that a slot of the batch uses
-      if (((m.x | (m.y & 0x7FFFFFFFu)) & s_act) != 0u) fan = __ldg(L.inv_off + i + 1) - __ldg(L.inv_off + i);
+      if (((m.x | (m.y & 0x7FFFFFFFu)) & act) != 0u) fan = __ldg(L.inv_off + i + 1) - __ldg(L.inv_off + i);
 #pragma unroll
-      for (int j = 0; j < 8; j++) inflight += h[j] < 255u + s_pmax ? 1u : 0u;
+      for (int j = 0; j < 8; j++) inflight += h[j] < 255u + pmax ? 1u : 0u;
     }
   }
   if (LEARN) learn_axons(L, i, A, fan, inflight);
@@ -566,9 +571,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
   }
   bool ev = false;
   if (i < N) {
-    const uint8_t t = timers[i];
-    if (t > 0) {                                  // physics.cu:168-174 after the burst reset
-      timers[i] = (uint8_t)(t - 1);
+    if (tm > 0) {                                 // physics.cu:168-174 after the burst reset
+      timers[i] = (uint8_t)(tm - 1);
       flags[i] = flags[i] & 0xF0;
     } else {
       ev = true;

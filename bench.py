@@ -507,10 +507,11 @@ def run_learned(args) -> None:
     """The learned schedule against the plain path on the same brain and ticks.
 
     Ticks [0, trace): dense with trace recording (200k tile-ticks), then GPU
-    training; [trace, trace+200): the predictor running but forced dense (its
-    overhead); [trace+200, total): the predictor's schedule.  The plain copy
-    of the brain runs the same ticks through axc_step_day_phase_batch; final
-    states are compared."""
+    training; [trace, total-200): the predictor's schedule (timed);
+    [total-200, total): the predictor running but the schedule forced dense
+    (the learned engine's cost over the plain path when it never goes
+    sparse, in the steady state).  The plain copy of the brain runs the same
+    ticks through axc_step_day_phase_batch; final states are compared."""
     import hashlib
     import torch
     import __graft_entry__ as G
@@ -577,21 +578,22 @@ def run_learned(args) -> None:
     loss, val = eng.train(epochs=args.learned_epochs, batch=1024, lr=2e-3, seed=7)
     train_s = time.perf_counter() - t0
     default = torch.cuda.default_stream()
-    # 2. the predictor's overhead: features + inference + plan, schedule forced dense
-    eng.set_policy(L.Policy(policy=-1, ratio=float("inf")))
-    t_over = timed(lambda: eng.run(trace, window, tpg), default)
-    t_plain_w = timed(lambda: plain_run(trace, window), ps)
-    # 3. the learned schedule
+    # 2. the learned schedule
     eng.set_policy(L.Policy(policy=-1, ratio=args.learned_ratio))
     eng.reset_stats()
-    t1 = trace + window
-    ticks = total - t1
+    t1 = trace
+    ticks = total - trace - window
     clocks = Clocks(0)
     clocks.start()
     t_learned = timed(lambda: eng.run(t1, ticks, tpg), default)
     t_plain = timed(lambda: plain_run(t1, ticks), ps)
     clk = clocks.stop()
     st = eng.stats()
+    # 3. the predictor running, schedule forced dense: the learned form's cost when it never goes sparse
+    t2 = t1 + ticks
+    eng.set_policy(L.Policy(policy=-1, ratio=float("inf")))
+    t_over = timed(lambda: eng.run(t2, window, tpg), default)
+    t_plain_w = timed(lambda: plain_run(t2, window), ps)
 
     def digest(v):
         h = hashlib.sha256()
