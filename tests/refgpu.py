@@ -81,8 +81,8 @@ class ReferenceKernels:
                                          None), name)
 
     def step(self, vram, padded_n, total_axons, v_seg, tick, d_bitmask, voff, nv, d_incoming, n_in, d_ids, d_out,
-             n_out, dopamine):
-        """physics.cu:441-495 with the reference's own kernels."""
+             n_out, dopamine, sync=True):
+        """physics.cu:441-495 with the reference's own kernels, on the legacy default stream."""
         u32 = C.c_uint32
         vp = vram.ptrs  # ShardVramPtrs (ctypes struct of 9 pointers), passed by value
         self._launch("reset", padded_n, [vp, u32(padded_n)])
@@ -97,4 +97,5 @@ class ReferenceKernels:
         if n_out > 0 and d_ids and d_out:
             self._launch("readout", n_out, [C.c_void_p(vp.soma_flags), C.c_void_p(d_ids), C.c_void_p(d_out),
                                             u32(n_out)])
-        self._chk(self.cu.cuCtxSynchronize(), "sync")
+        if sync:
+            self._chk(self.cu.cuCtxSynchronize(), "sync")

@@ -6,6 +6,8 @@ result depends on whether such a push was already visible is "race-exposed".
 The oracle fixes snapshot semantics, so it must agree with the reference on
 every neuron that is not race-exposed, every tick.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -125,4 +127,79 @@ def test_oracle_matches_reference_kernels(gpu, case):
     finally:
         for p in (d_bm, d_ids, d_out, d_in):
             lib.gpu_free(p)
+        vram.free()
+
+
+def test_reference_kernels_against_batch_path_on_config1(gpu):
+    """The reference's own Day Phase kernels (physics.cu compiled for sm_103a, launched in
+    cu_step_day_phase's order) and this engine's batch path on the 1.5M brain in its steady state
+    (after 700 ticks), the same 100 ticks from the same state on the same GPU, timed with CUDA
+    events on each launching stream.  Prints one JSON line; the engine must be faster."""
+    if not refgpu.available():
+        pytest.skip("reference cubin absent (built from the reference sources by oracle/build_ref.py)")
+    import json
+    import torch
+    w = W.config1()
+    lay, state, heads = S.generate_brain(w.spec())
+    S.upload_lut(w.lut)
+    Np, A = lay.padded_n, lay.total_axons
+    vram = S.VramState(Np, A)
+    vram.upload_state(state)
+    vram.upload_axon_heads(heads)
+    del state, heads
+    eng = S.ShardEngine(vram)
+    lib = N.lib()
+    words = (w.num_inputs + 31) // 32
+    warm, T = 700, 100
+    bm = S.input_bitmask(w.seed, 0, warm + T, w.num_inputs, w.rate_q32)
+    io = S.IoDeviceBuffers(words, 0, 0, 100)
+    for t in range(0, warm, 100):
+        eng.step_day_phase_batch(100, io, bm[t * words:(t + 100) * words], None, None, lay.virtual_offset,
+                                 w.num_inputs, None, 1, 0, t)
+    eng.synchronize()
+    st0, hd0 = vram.download_state(), vram.download_heads()
+    rows = bm[warm * words:(warm + T) * words]
+    d_bm = S.device_array(rows)
+    try:
+        # this engine: one batch of T ticks through axc_step_day_phase_batch (graph captured first, untimed)
+        eng.step_day_phase_batch(T, io, rows, None, None, lay.virtual_offset, w.num_inputs, None, 1, 0, warm)
+        eng.synchronize()
+        vram.upload_state(st0)
+        vram.upload_axon_heads(hd0)
+        es = torch.cuda.ExternalStream(eng.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(es)
+        assert lib.axc_step_day_phase_batch(C.byref(vram.ptrs), Np, A, T, C.byref(io.as_struct()), d_bm, None,
+                                            None, lay.virtual_offset, w.num_inputs, None, 1, 0, warm, None,
+                                            eng.stream) == 0
+        e1.record(es)
+        torch.cuda.synchronize()
+        ours_s = e0.elapsed_time(e1) / 1e3
+        # the reference's kernels: the same ticks from the same state, on the legacy default stream
+        vram.upload_state(st0)
+        vram.upload_axon_heads(hd0)
+        rk = refgpu.ReferenceKernels()
+        rk.upload_lut(w.lut)
+        rk.step(vram, Np, A, 1, warm, d_bm, lay.virtual_offset, w.num_inputs, None, 0, None, None, 0, 0)  # warm
+        vram.upload_state(st0)
+        vram.upload_axon_heads(hd0)
+        default = torch.cuda.default_stream()
+        torch.cuda.synchronize()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(default)
+        for k in range(T):
+            rk.step(vram, Np, A, 1, warm + k, d_bm + k * words * 4, lay.virtual_offset, w.num_inputs, None, 0,
+                    None, None, 0, 0, sync=False)
+        r1.record(default)
+        torch.cuda.synchronize()
+        ref_s = r0.elapsed_time(r1) / 1e3
+        synapses = int(np.count_nonzero(StateView(st0, Np).targets))
+        print(json.dumps({"workload": "plain-1.5M", "ticks": [warm, warm + T],
+                          "reference_kernels_ticks_per_s": T / ref_s,
+                          "reference_kernels_events_per_s": T * synapses / ref_s,
+                          "engine_ticks_per_s": T / ours_s, "engine_events_per_s": T * synapses / ours_s,
+                          "speedup": ref_s / ours_s}))
+        assert ours_s < ref_s
+    finally:
+        lib.gpu_free(d_bm)
         vram.free()
