@@ -143,6 +143,18 @@ class Clocks:
 TRAFFIC = {("plain-1.5M", "k_rows_update"): 337.3e6}
 
 
+def cpu_model() -> str | None:
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+    except (OSError, subprocess.SubprocessError):
+        return None
+    for line in out.splitlines():
+        if line.startswith("Model name:"):
+            return line.split(":", 1)[1].strip()
+    return None
+
+
 def workload(name: str):
     from axicor_gb300 import workloads as W
     return getattr(W, CONFIGS[name])()
@@ -402,7 +414,7 @@ def run_reference(args, dist: Dist) -> None:
         "data": "synthetic (seeded generator)", "ticks_per_s": tps,
         "config": {"workload": args.workload, "neurons": lay.num_neurons, "synapses": synapses,
                    "ticks_per_step": per_step, "pre_ticks_untimed": pre, "parallelism": "replicas"},
-        "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "cpu_model": cpu_model(), "kind": "port",
                          "sample": f"{args.steps} ticks of the {args.workload} brain after {pre + args.warmup} "
                                    f"untimed ticks, C restatement of physics.cu with OpenMP"},
         "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -658,7 +670,8 @@ def main():
             st, hd = vram.download_state(), vram.download_heads()
             threads = os.cpu_count() or 1
             cs = cpu_sample(w, st, hd, lay, 10 ** 6, args.cpu_sample_s, threads)
-            cpu = {"value": cs["ticks_per_s"] * r["synapses"], "unit": "events/s", "cores": threads, "kind": "port",
+            cpu = {"value": cs["ticks_per_s"] * r["synapses"], "unit": "events/s", "cores": threads,
+                   "cpu_model": cpu_model(), "kind": "port",
                    "sample": f"{cs['ticks']} ticks ({cs['seconds']:.1f} s) of the {args.workload} brain from the "
                              f"GPU's state after the timed region; C restatement of physics.cu, OpenMP",
                    "ticks_per_s": cs["ticks_per_s"]}
