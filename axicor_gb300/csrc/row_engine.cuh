@@ -487,9 +487,11 @@ __device__ __forceinline__ void learn_axons(const LearnDev& L, uint32_t i, uint3
 }
 
 // ---------------------------------------------------------------------------
-// per tick 1/4: axons (inject, network pushes, propagate, split masks) and
-// somas (refractory countdown, list of neurons to evaluate).  The list entry
-// positions are reserved once per block.
+// per tick 1/4 of the learned engine (LEARN): axons (inject, network pushes,
+// propagate, split masks) and somas (refractory countdown, list of neurons to
+// evaluate), with learn_axons' per-tile activity and, on sparse ticks, the
+// compaction of the active axons.  The list entry positions are reserved once
+// per block.  The plain engine runs k_rows_prologue_plain.
 // ---------------------------------------------------------------------------
 template <bool LEARN>
 __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__ heads, uint32_t A, uint32_t v_seg,
@@ -1083,13 +1085,14 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
 }
 
 // ---------------------------------------------------------------------------
-// per tick 2b: GSOP (physics.cu:281-373) of the listed spikers over the slots
-// of amask only (the others are frozen: GSOP leaves them as they are), the
-// (spiker, slot) items of 32 spikers spread over the warp's lanes.  Each slot is classified as in the update pass (fully lit,
+// per tick 2b (learned engine): GSOP (physics.cu:281-373) of the listed
+// spikers over the slots of amask only (the others are frozen: GSOP leaves
+// them as they are), the (spiker, slot) items of 32 spikers spread over the
+// warp's lanes.  Each slot is classified as in the update pass (fully lit,
 // else the tick's hit masks; exact path for segments >= 31, other lengths,
 // several owners, or a hit that one same-tick push could change) and updated
 // from the gtab deltas, on the exact path, or deferred to the fix-up stage.
-// Warp w of the update pass listed its spikers at [beg_w, beg_w + wcnt[w]).
+// Warp w of the listing pass listed its spikers at [beg_w, beg_w + wcnt[w]).
 // ---------------------------------------------------------------------------
 template <bool LIT>
 __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
@@ -1345,8 +1348,9 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
   }
 }
 
-// per tick 4/4: the spikers' own-axon pushes (physics.cu:257-261), found in
-// the evaluated list; readout (physics.cu:378-395); the next tick's lists.
+// per tick 4/4, on a batch's (or learned graph's) last tick: the spikers'
+// own-axon pushes (physics.cu:257-261), found in the evaluated list; on the
+// other ticks the next prologue applies them.
 __global__ void __launch_bounds__(256) k_rows_push(BurstHeads8* __restrict__ heads, const uint32_t* __restrict__ s2a,
                                                    uint32_t A, uint32_t* __restrict__ pend,
                                                    const uint32_t* __restrict__ eval, const uint8_t* __restrict__ flags,
@@ -1396,11 +1400,12 @@ __global__ void k_rows_reset_lists(ShardCtl* ctl) {
 }
 
 // ---------------------------------------------------------------------------
-// per tick 1/4 of the plain engine: the work of k_rows_prologue<false> with
-// ITEMS axons and neurons per thread (items i0 + 256 r).  No barrier before
-// the loads: every thread reads the batch constants (seg_max, the LUT's
-// largest length, set at batch start) itself, next to its own loads.  The
-// evaluated neurons are appended with one atomic per block.
+// per tick 1/4 of the plain engine: k_rows_prologue without the learned
+// engine's per-tile accounting, ITEMS axons and neurons per thread (items
+// i0 + 256 r).  No barrier before the loads: every thread reads the batch
+// constants (seg_max, the LUT's largest length, set at batch start) itself,
+// next to its own loads.  The evaluated neurons are appended with one atomic
+// per block.
 // ---------------------------------------------------------------------------
 // push_n for the common counts 0 and 1 without the general shift network
 __device__ __forceinline__ void push_few(uint32_t h[8], uint32_t c) {
