@@ -34,9 +34,11 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 CONFIGS = {"plain-1.5M": "config1", "plain-16k": "config0", "plain-8M": "config4"}
-# learned-schedule workloads: the 1.5M brain as configured (saturated dynamics),
-# and the same brain with homeostasis on and the 0.01..0.2 sinusoidal input (quiet)
-LEARNED = {"learned-1.5M": False, "learned-homeostatic-1.5M": True}
+# learned-schedule workloads (brain, homeostatic): the 1.5M brain as configured (saturated
+# dynamics), the same brain with homeostasis on and the 0.01..0.2 sinusoidal input (quiet), and
+# the 8M brain as configured
+LEARNED = {"learned-1.5M": ("config1", False), "learned-homeostatic-1.5M": ("config1", True),
+           "learned-8M": ("config4", False)}
 
 
 def parse():
@@ -534,8 +536,9 @@ def run_learned(args) -> None:
     from axicor_gb300 import workloads as W
     lib = N.lib()
     lib.gpu_set_device(0)
-    w = W.config1()
-    if LEARNED[args.workload]:
+    brain, quiet = LEARNED[args.workload]
+    w = getattr(W, brain)()
+    if quiet:
         w = W.homeostatic(w)
     tpg = args.ticks_per_step
     total = args.learned_ticks
