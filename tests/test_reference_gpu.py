@@ -130,16 +130,17 @@ def test_oracle_matches_reference_kernels(gpu, case):
         vram.free()
 
 
-def test_reference_kernels_against_batch_path_on_config1(gpu):
+@pytest.mark.parametrize("config", ["config1", "config0"])
+def test_reference_kernels_against_batch_path_on_config1(gpu, config):
     """The reference's own Day Phase kernels (physics.cu compiled for sm_103a, launched in
-    cu_step_day_phase's order) and this engine's batch path on the 1.5M brain in its steady state
-    (after 700 ticks), the same 100 ticks from the same state on the same GPU, timed with CUDA
-    events on each launching stream.  Prints one JSON line; the engine must be faster."""
+    cu_step_day_phase's order) and this engine's batch path on the 1.5M brain (and the 16k brain) in
+    its steady state (after 700 ticks), the same 100 ticks from the same state on the same GPU, timed
+    with CUDA events on each launching stream.  Prints one JSON line; the engine must be faster."""
     if not refgpu.available():
         pytest.skip("reference cubin absent (built from the reference sources by oracle/build_ref.py)")
     import json
     import torch
-    w = W.config1()
+    w = getattr(W, config)()
     lay, state, heads = S.generate_brain(w.spec())
     S.upload_lut(w.lut)
     Np, A = lay.padded_n, lay.total_axons
@@ -194,7 +195,7 @@ def test_reference_kernels_against_batch_path_on_config1(gpu):
         torch.cuda.synchronize()
         ref_s = r0.elapsed_time(r1) / 1e3
         synapses = int(np.count_nonzero(StateView(st0, Np).targets))
-        print(json.dumps({"workload": "plain-1.5M", "ticks": [warm, warm + T],
+        print(json.dumps({"workload": w.name, "ticks": [warm, warm + T],
                           "reference_kernels_ticks_per_s": T / ref_s,
                           "reference_kernels_events_per_s": T * synapses / ref_s,
                           "engine_ticks_per_s": T / ours_s, "engine_events_per_s": T * synapses / ours_s,
