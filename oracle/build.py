@@ -1,7 +1,7 @@
 """Builds the CPU oracle ``oracle/_build/liboracle.so`` (test infrastructure).
 
-Plain gcc, OpenMP, no host-specific flags, so the same recipe builds on the
-x86-64 development host and on the aarch64 GPU host.
+Plain gcc, OpenMP, no host-specific flags, so the same recipe builds the same
+arithmetic on x86-64 and on aarch64 hosts.
 """
 from __future__ import annotations
 

@@ -6,8 +6,8 @@ For each case: the seeded brain is generated, its .state/.axons hashes are
 recorded, then the oracle runs the batch loop (genesis-compute/src/compute/shard.rs:40-124)
 with the case's seeded inputs; per-tick spike counts, the SHA-256 of the
 whole spike raster and of the final .state/.axons bytes are stored.  The
-tests re-derive these on the CPU and compare the GPU engine's output with
-them on the GPU host.
+tests re-derive these on the CPU, and the GPU tests compare the engine's
+output with them.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 """The generator and the oracle reproduce the committed golden traces (tests/golden/).
 
 The traces were produced by tests/golden/make_golden.py; the GPU tests compare
-the engine's output on the GPU host with the same files.
+the engine's output with the same files.
 """
 import json
 from pathlib import Path
