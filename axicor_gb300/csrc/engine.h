@@ -4,9 +4,29 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <tuple>
+#include <type_traits>
+#include <utility>
+
 #include "../../include/axicor_day.h"
 
 namespace axc {
+
+// Launches kernel k and returns the status of that launch alone
+// (cudaLaunchKernel's return value), without reading or clearing an error
+// that an earlier call left pending.  Arguments convert to the kernel's
+// parameter types.
+template <typename... P, typename... A, size_t... I>
+cudaError_t launch_k_impl(void (*k)(P...), dim3 g, dim3 b, cudaStream_t s, std::index_sequence<I...>, A&&... a) {
+  std::tuple<std::decay_t<P>...> t(static_cast<std::decay_t<P>>(std::forward<A>(a))...);
+  void* args[sizeof...(P) > 0 ? sizeof...(P) : 1] = {static_cast<void*>(&std::get<I>(t))...};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(k), g, b, args, 0, s);
+}
+template <typename... P, typename... A>
+cudaError_t launch_k(void (*k)(P...), dim3 g, dim3 b, cudaStream_t s, A&&... a) {
+  static_assert(sizeof...(P) == sizeof...(A), "one argument per kernel parameter");
+  return launch_k_impl(k, g, b, s, std::index_sequence_for<P...>{}, std::forward<A>(a)...);
+}
 
 // Control block of one shard in device memory.
 struct ShardCtl {

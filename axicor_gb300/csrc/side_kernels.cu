@@ -338,6 +338,9 @@ void launch_extract_outgoing_spikes(const BurstHeads8* axon_heads, const uint32_
   }
   const uint32_t nb = (count + kExtBlock - 1) / kExtBlock;
   uint32_t* tmp = nullptr;
+  // bindings.cu:431 clears the count before anything else: a call that fails
+  // to get its scratch then reports 0 events, not the previous batch's count
+  cudaMemsetAsync(out_count, 0, sizeof(uint32_t), stream);
   if (cudaMallocAsync(&tmp, (size_t)nb * 4, stream) != cudaSuccess) return;
   k_ext_count<<<nb, kExtBlock, 0, stream>>>(axon_heads, src_indices, count, sync_batch_ticks, v_seg, tmp);
   k_scan_totals<<<1, 1024, 0, stream>>>(tmp, nb, out_count, 0);
@@ -366,16 +369,24 @@ int32_t axc_extract_outgoing_spikes_noalloc(const BurstHeads8* axon_heads, const
   cudaError_t e = noalloc_scratch(&totals);
   if (e != cudaSuccess) return (int32_t)e;
   cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  // Each launch reports its own status (cudaLaunchKernel's return), so an
+  // error left pending by an earlier, unrelated call is neither blamed on this
+  // one nor cleared: the caller still reads it with cudaGetLastError.
   if (count == 0 || v_seg == 0) {
-    k_scan_totals<<<1, 1024, 0, stream>>>(totals, 0, out_count, 0);   // writes *out_count = 0
-    return (int32_t)cudaGetLastError();
+    uint32_t zero = 0;
+    int acc = 0;
+    return (int32_t)launch_k(k_scan_totals, dim3(1), dim3(1024), stream, totals, zero, out_count, acc);  // *out_count = 0
   }
-  const uint32_t nb = (count + kExtBlock - 1) / kExtBlock;
-  k_ext_count<<<nb, kExtBlock, 0, stream>>>(axon_heads, src_indices, count, sync_batch_ticks, v_seg, totals);
-  k_scan_totals<<<1, 1024, 0, stream>>>(totals, nb, out_count, 0);
-  k_ext_write<<<nb, kExtBlock, 0, stream>>>(axon_heads, src_indices, dst_ghost_ids, count, sync_batch_ticks, v_seg,
-                                            totals, static_cast<SpikeEvent*>(out_events));
-  return (int32_t)cudaGetLastError();
+  uint32_t nb = (count + kExtBlock - 1) / kExtBlock;
+  int acc = 0;
+  SpikeEvent* events = static_cast<SpikeEvent*>(out_events);
+  e = launch_k(k_ext_count, dim3(nb), dim3(kExtBlock), stream, axon_heads, src_indices, count, sync_batch_ticks, v_seg,
+               totals);
+  if (e == cudaSuccess) e = launch_k(k_scan_totals, dim3(1), dim3(1024), stream, totals, nb, out_count, acc);
+  if (e == cudaSuccess)
+    e = launch_k(k_ext_write, dim3(nb), dim3(kExtBlock), stream, axon_heads, src_indices, dst_ghost_ids, count,
+                 sync_batch_ticks, v_seg, static_cast<const uint32_t*>(totals), events);
+  return (int32_t)e;
 }
 
 // bindings.cu:780-782 is a no-op in the reference; so is this.

@@ -140,8 +140,8 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-# DRAM traffic per launch of the dominant kernel from one ncu capture of the same kernel on the same
-# workload in its steady state (profiles/k_rows_update_plain-1.5M.md)
+# DRAM traffic per launch of the dominant kernel (ncu dram__bytes_read.sum + dram__bytes_write.sum) from one
+# capture of the same kernel on the same workload in its steady state
 TRAFFIC = {("plain-1.5M", "k_rows_update"): 337.3e6}
 
 
@@ -415,7 +415,8 @@ def run_reference(args, dist: Dist) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator)", "ticks_per_s": tps,
         "config": {"workload": args.workload, "neurons": lay.num_neurons, "synapses": synapses,
-                   "ticks_per_step": per_step, "pre_ticks_untimed": pre, "parallelism": "replicas"},
+                   "ticks_per_step": per_step, "pre_ticks_untimed": pre,
+                   "parallelism": "single" if dist.world == 1 else "replicas"},
         "cpu_baseline": {"value": v, "unit": "events/s", "cores": threads, "cpu_model": cpu_model(), "kind": "port",
                          "sample": f"{args.steps} ticks of the {args.workload} brain after {pre + args.warmup} "
                                    f"untimed ticks, C restatement of physics.cu with OpenMP"},

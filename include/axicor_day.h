@@ -311,9 +311,13 @@ int32_t axc_shard_counters(const ShardVramPtrs* vram, uint32_t reset, uint64_t o
  * AXC_NOALLOC_MAX_BOUNDARY_AXONS boundary axons per call, and a larger
  * `count` returns cudaErrorInvalidValue without launching anything.
  * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU (two streams, two threads) race and must be
- * serialised by the caller.  Returns 0 or a cudaError_t. */
+ * first call before any stream capture.  The address is kept for the life of
+ * the process: after cudaDeviceReset it is stale, so a process that resets
+ * a device must not call this entry point on that device again.  All calls
+ * share the array: calls that overlap on the GPU (two streams, two threads)
+ * race and must be serialised by the caller.  Returns 0 or the cudaError_t
+ * of this call's own launches (an error left pending by an earlier call is
+ * neither returned nor cleared). */
 #define AXC_NOALLOC_MAX_BOUNDARY_AXONS (1u << 20)
 int32_t axc_extract_outgoing_spikes_noalloc(const BurstHeads8* axon_heads,
                                             const uint32_t* src_indices,
