@@ -178,6 +178,8 @@ SIGNATURES: dict[str, tuple] = {
     "axc_profile_ticks": (I32, [PV, U32, U32, U32, U32, U32, P, U32, U32, U32, I16, I32, P, C.POINTER(C.c_float),
                                 C.POINTER(C.c_uint64)]),
     "axc_batch_engine_mode": (I32, [I32]),
+    "axc_tick_engine_mode": (I32, [I32]),
+    "axc_shard_invalidate": (I32, [PV]),
     "axc_row_engine_fix_capacity": (U32, [U32]),
     "axc_extract_outgoing_spikes_noalloc": (I32, [P, P, P, U32, U32, U32, P, P, P]),
     "axc_population_create": (I32, [P, U32, C.POINTER(P)]),

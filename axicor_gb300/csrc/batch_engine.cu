@@ -74,6 +74,16 @@ void graph_cache_free(ShardScratch* s) {
   s->graph_cache = nullptr;
 }
 
+void graph_cache_drop(ShardScratch* s) {
+  if (!s || !s->graph_cache) return;
+  GraphCache* c = static_cast<GraphCache*>(s->graph_cache);
+  std::lock_guard<std::mutex> lk(c->mu);
+  for (auto& kv : c->execs) cudaGraphExecDestroy(kv.second);
+  c->execs.clear();
+}
+
+uint32_t fix_capacity() { return g_fix_cap.load(); }
+
 }  // namespace axc
 
 using namespace axc;
@@ -100,6 +110,7 @@ extern "C" int32_t axc_step_day_phase_batch(const ShardVramPtrs* vram, uint32_t 
   cudaError_t e;
   ShardScratch* s = scratch_for(vram, padded_n, total_axons, &e);
   if (!s) return (int32_t)e;
+  rows_touched(*s);   // the batch's row copy replaces the per-tick entry point's
   // Captured graphs hold the addresses of the scratch buffers: any
   // reallocation below drops them.
   bool realloc = false;
@@ -219,6 +230,7 @@ extern "C" int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_
   if (!s) return (int32_t)e;
   const bool rows = engine == 1;
   cudaStream_t st = static_cast<cudaStream_t>(stream_v);
+  rows_touched(*s);
   if (rows) {
     bool realloc = false;
     e = ensure_counts(*s, ticks ? ticks : 1, &realloc);

@@ -532,7 +532,12 @@ int sm_count() {
   return cached;
 }
 
+static std::atomic<uint64_t> g_lut_gen{1};
+
+uint64_t lut_generation() { return g_lut_gen.load(); }
+
 cudaError_t lut_upload(const VariantParameters* lut, cudaStream_t stream, bool async) {
+  g_lut_gen.fetch_add(1);   // row caches built from the previous LUT (frozen ranks, Pmax) are stale
   if (async)
     return cudaMemcpyToSymbolAsync(VARIANT_LUT, lut, sizeof(VariantParameters) * 16, 0,
                                    cudaMemcpyHostToDevice, stream);

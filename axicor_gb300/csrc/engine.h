@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <tuple>
 #include <type_traits>
 #include <utility>
@@ -82,12 +83,22 @@ struct ShardScratch {
   uint32_t* h_counts_pinned = nullptr;  // pinned staging for batch_counts / tick_base
   void* graph_cache = nullptr;          // batch engine graphs (batch_engine.cu)
   RowCache* rows = nullptr;             // batch engine neuron-major dendrites
+  // Per-tick entry point (cu_step_day_phase): its row cache lives across calls.
+  // It is valid while nothing else wrote the shard's targets, weights, flags or
+  // soma_to_axon and the LUT is the one it was built with; every entry point
+  // of this library that writes them clears the flag.
+  std::atomic<bool> tick_rows_valid{false};
+  uint64_t tick_rows_lut = 0;           // LUT generation the per-tick row cache was built with
+  uint32_t tick_parity = 0;             // per-tick calls alternate the row engine's list slots
+  const void* state_base = nullptr;     // the shard's .state allocation (invalidation by address)
+  size_t state_bytes = 0;
 };
 
 constexpr uint32_t kFixCap = 1u << 22;  // deferred GSOP slots per tick before the rescan path
 constexpr uint32_t kMaxUpdateWarps = 32u * 1024u;  // warps of the update pass (32 per SM)
 
-// Row engine (row_engine.cuh, compiled in day_phase.cu).
+// Row engine (row_engine.cuh, compiled in day_phase.cu).  A (re)allocation
+// drops the batch engine's captured graphs, which hold the old addresses.
 cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix = true);
 void rows_free(ShardScratch& s);
 // row_sum: also compute the targets checksum (ShardCtl::row_sum) the learned engine checks its index against.
@@ -101,6 +112,15 @@ ShardScratch* scratch_for(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
                           cudaError_t* err);
 void scratch_release(const void* heads_key);
 void graph_cache_free(ShardScratch* s);  // batch_engine.cu
+void graph_cache_drop(ShardScratch* s);  // batch_engine.cu: destroys the captured graphs only
+uint32_t fix_capacity();                 // batch_engine.cu: deferred-GSOP list capacity in use
+
+// The per-tick row cache of a shard no longer matches its memory (shard_api.cu).
+inline void rows_touched(ShardScratch& s) { s.tick_rows_valid.store(false); }
+// Marks every shard whose .state allocation overlaps [dst, dst + size).
+void invalidate_overlapping(const void* dst, size_t size);
+// Looks up a shard's scratch without creating it (nullptr if none).
+ShardScratch* scratch_find(const ShardVramPtrs* vram);
 
 // Tick stages (day_phase.cu).  When dctl_batch is true the tick number,
 // dopamine and network spike count come from the shard's device control
@@ -142,8 +162,10 @@ cudaError_t launch_update_stage(const ShardVramPtrs& v, ShardScratch& s, uint32_
 cudaError_t launch_gsop_stage(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, int16_t dopamine,
                               cudaStream_t stream);
 
-// LUT access for host code (day_phase.cu owns the __constant__ symbol).
+// LUT access for host code (day_phase.cu owns the __constant__ symbol).  Every
+// upload advances the LUT generation.
 cudaError_t lut_upload(const VariantParameters* lut, cudaStream_t stream, bool async);
+uint64_t lut_generation();
 
 int sm_count();
 

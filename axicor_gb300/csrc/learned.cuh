@@ -843,6 +843,7 @@ static cudaError_t learned_index(Learned& L, cudaStream_t st) {
   if (!s) return e;
   e = rows_alloc(*s, L.N, L.A);
   if (e != cudaSuccess) return e;
+  rows_touched(*s);   // slot-order rows replace the per-tick entry point's
   e = launch_rows_begin(L.v, *s, L.N, L.A, st, true, false);
   if (e != cudaSuccess) return e;
   const RowCache& r = *s->rows;
@@ -922,7 +923,7 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool la
                                                            raise, r.lit, D, k > 0 ? s.pend : nullptr);
   learned_update_forms(L, s, k, st);
   k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k,
-                                        nullptr, nullptr, 0);
+                                        nullptr, nullptr, 0, ColWT{});
   // soma pushes: by the next tick's prologue within a graph, here on its last tick
   if (last)
     k_rows_push<<<2 * sms, 256, 0, st>>>(L.v.axon_heads, L.v.soma_to_axon, A, s.pend, r.eval, L.v.soma_flags, N,
@@ -1098,6 +1099,7 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   if (!s) return (int32_t)e;
   e = rows_alloc(*s, L->N, L->A);
   if (e != cudaSuccess) return (int32_t)e;
+  rows_touched(*s);
   if (L->rows_base != s->rows->base) {
     L->drop_graphs();
     L->rows_base = s->rows->base;

@@ -619,6 +619,7 @@ struct Population {
   uint32_t chunk = kPopChunk;
   uint32_t lit_cap = 0;   // words of the largest fully-lit bitmap the update stages (<= kPopLitWords)
   std::vector<uint32_t> bm_ticks;   // per brain: bitmask rows (UINT32_MAX without a bitmask)
+  std::vector<ShardScratch*> scr;   // per brain: the shard's scratch (its rows are this engine's while it runs)
   std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t>, cudaGraphExec_t> graphs;
   cudaStream_t capture = nullptr;
 };
@@ -702,6 +703,8 @@ int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, voi
     if (!s) break;
     e = rows_alloc(*s, d.padded_n, d.total_axons, false);
     if (e != cudaSuccess) break;
+    rows_touched(*s);
+    P->scr.push_back(s);
     PopBrain& h = P->hb[b];
     std::memset(&h, 0, sizeof(h));
     h.P = d.vram;
@@ -772,6 +775,7 @@ int32_t axc_population_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_
   Population* P = static_cast<Population*>(handle);
   if (!P || tpg == 0 || ticks % tpg || !pop_ticks_ok(*P, tick0, ticks)) return (int32_t)cudaErrorInvalidValue;
   cudaStream_t st = static_cast<cudaStream_t>(stream_v);
+  for (ShardScratch* s : P->scr) rows_touched(*s);   // the per-tick entry point's row copies are replaced
   auto key = std::make_tuple(tpg, P->sched.lanes_per_neuron, P->sched.update_blocks_per_sm,
                              P->sched.aux_blocks_per_sm * 1000 + std::min(g_pop_fix_cap(), kFixCap) % 1000);
   cudaGraphExec_t exec = nullptr;

@@ -97,6 +97,46 @@ __device__ __forceinline__ void md_pair(const BurstHeads8* heads, uint32_t a, ui
   *md1 = min(m06, dz < len ? dz : kInf);
 }
 
+// Write-through of GSOP's weight changes to the reference's columnar blob
+// (dendrite_weights[slot][N]), used by the per-tick entry point, whose row
+// cache outlives the call: after every tick the blob must hold the weights the
+// reference would hold.  w == nullptr: no write-through (the batch paths write
+// every weight back at batch end).
+struct ColWT {
+  int16_t* w = nullptr;         // columnar weights of the shard
+  const uint4* om = nullptr;    // per neuron: the columnar slots placed first in its row
+  const uint16_t* cnt = nullptr;
+  uint32_t N = 0;
+};
+
+// The r-th set bit (0-based) of a 128-bit mask.
+__device__ __forceinline__ uint32_t nth_bit128(uint4 m, uint32_t r) {
+  const uint32_t c0 = __popc(m.x);
+  if (r < c0) return __fns(m.x, 0, r + 1);
+  r -= c0;
+  const uint32_t c1 = __popc(m.y);
+  if (r < c1) return 32u + __fns(m.y, 0, r + 1);
+  r -= c1;
+  const uint32_t c2 = __popc(m.z);
+  if (r < c2) return 64u + __fns(m.z, 0, r + 1);
+  return 96u + __fns(m.w, 0, r - c2 + 1);
+}
+
+// Columnar slot of row position pos in a row of c used slots whose slots of om
+// come first (in slot order) and the other used slots after them (in slot order).
+__device__ __forceinline__ uint32_t col_of_pos(uint4 om, uint32_t pos, uint32_t c) {
+  const uint32_t olf = __popc(om.x) + __popc(om.y) + __popc(om.z) + __popc(om.w);
+  if (pos < olf) return nth_bit128(om, pos);
+  const auto used = [c](uint32_t lo) { return c >= lo + 32u ? 0xFFFFFFFFu : (c > lo ? (1u << (c - lo)) - 1u : 0u); };
+  const uint4 rest = make_uint4(used(0) & ~om.x, used(32) & ~om.y, used(64) & ~om.z, used(96) & ~om.w);
+  return nth_bit128(rest, pos - olf);
+}
+
+__device__ __forceinline__ void col_write(const ColWT& wt, uint32_t n, uint32_t pos, int16_t w) {
+  const uint32_t q = col_of_pos(wt.om[n], pos, wt.cnt[n] & 0xFFu);
+  wt.w[(size_t)q * wt.N + n] = w;
+}
+
 // Per-neuron GSOP constants (physics.cu:290-345).
 struct GsopConsts {
   int32_t bm, raw_pot, final_dep;
@@ -872,7 +912,8 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
                                              uint32_t var, const uint32_t* rt_n, int16_t* rw_n,
                                              const BurstHeads8* heads, const uint2* mask2, uint32_t A,
                                              const VariantParameters& p, uint8_t flags, int32_t dopamine,
-                                             ShardCtl* ctl, uint32_t* fix, uint32_t fix_cap, uint32_t n) {
+                                             ShardCtl* ctl, uint32_t* fix, uint32_t fix_cap, uint32_t n,
+                                             const ColWT& wt = ColWT{}) {
   uint32_t gdone = 0;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
@@ -909,7 +950,14 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
       }
       set_half(wj, i, nw);
     }
-    if (wj.x != W[j].x || wj.y != W[j].y) *reinterpret_cast<uint2*>(rw_n + q0) = wj;
+    if (wj.x != W[j].x || wj.y != W[j].y) {
+      *reinterpret_cast<uint2*>(rw_n + q0) = wj;
+      if (wt.w) {
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          if (half_of(wj, i) != half_of(W[j], i)) col_write(wt, n, q0 + i, half_of(wj, i));
+      }
+    }
   }
   if (sh.F < 4u) {
 #pragma unroll
@@ -940,7 +988,10 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
           continue;
         }
       }
-      if (nw != w16) rw_n[q] = nw;
+      if (nw != w16) {
+        rw_n[q] = nw;
+        if (wt.w) col_write(wt, n, q, nw);
+      }
     }
   }
   return gdone;
@@ -959,7 +1010,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
                   const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend, uint32_t* __restrict__ fix,
                   ShardCtl* __restrict__ ctl, uint32_t k, uint32_t fix_cap, const uint32_t* __restrict__ lit_bits,
                   const LearnCtl* __restrict__ lc, uint32_t* __restrict__ gs_n, uint32_t* __restrict__ gd_n,
-                  const uint8_t* __restrict__ lfz, uint32_t* __restrict__ wcnt) {
+                  const uint8_t* __restrict__ lfz, uint32_t* __restrict__ wcnt, ColWT wt) {
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
@@ -1054,7 +1105,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
         // of its row; frozen slots (GSOP leaves them as they are) are counted
         if (spike && lf > 0u)
           gdone += row_gsop(W, hitb, slowb, lf, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
-                            dopamine, ctl, fix, fix_cap, n);
+                            dopamine, ctl, fix, fix_cap, n, wt);
         if (spike && g8 == 0) gdone += c - lf;
         continue;
       }
@@ -1269,7 +1320,7 @@ __global__ void __launch_bounds__(256) k_rows_gsop_rows(ShardVramPtrs P, uint32_
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void fixup_slot(const ShardVramPtrs& P, const VariantParameters* lut, uint32_t A,
                                            const uint32_t* rt, int16_t* rw, const uint32_t* pend,
-                                           uint32_t r, int32_t dopamine) {
+                                           uint32_t r, int32_t dopamine, const ColWT& wt = ColWT{}) {
   const uint32_t n = r / kRowStride;
   const uint32_t t = rt[r];
   const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
@@ -1281,7 +1332,12 @@ __device__ __forceinline__ void fixup_slot(const ShardVramPtrs& P, const Variant
   push_n(h, pend[a]);
   const uint32_t md = md_of(h, s, p.signal_propagation_length);
   const GsopConsts gc = gsop_consts(flags, p, dopamine);
-  rw[r] = gsop_weight(rw[r], md, p, gc.bm, gc.raw_pot, gc.final_dep);
+  const int16_t w0 = rw[r];
+  const int16_t w1 = gsop_weight(w0, md, p, gc.bm, gc.raw_pot, gc.final_dep);
+  if (w1 != w0) {
+    rw[r] = w1;
+    if (wt.w) col_write(wt, n, r % kRowStride, w1);
+  }
 }
 
 __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N, uint32_t A,
@@ -1291,7 +1347,7 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
                                                     const uint32_t* __restrict__ eval,
                                                     const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
                                                     uint32_t k, const uint32_t* __restrict__ ids,
-                                                    uint8_t* __restrict__ out, uint32_t num_outputs) {
+                                                    uint8_t* __restrict__ out, uint32_t num_outputs, ColWT wt) {
   const uint32_t nfix = ctl->fix_count;
   const uint32_t overflow = ctl->fix_overflow;
   {
@@ -1321,7 +1377,7 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (!overflow) {
-    for (uint32_t i = tid; i < nfix; i += stride) fixup_slot(P, lut, A, rt, rw, pend, fix[i], dopamine);
+    for (uint32_t i = tid; i < nfix; i += stride) fixup_slot(P, lut, A, rt, rw, pend, fix[i], dopamine, wt);
     return;
   }
   // the list overflowed: rescan every spiker's slots with the update pass's rule
@@ -1344,7 +1400,7 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
     if (fast) continue;
     uint32_t md0, md1;
     md_pair(P.axon_heads, a, s, prop, &md0, &md1);
-    if ((m.y >> 31) || md0 != md1) fixup_slot(P, lut, A, rt, rw, pend, r, dopamine);
+    if ((m.y >> 31) || md0 != md1) fixup_slot(P, lut, A, rt, rw, pend, r, dopamine, wt);
   }
 }
 
@@ -1430,7 +1486,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
                                                              uint8_t* __restrict__ timers, uint32_t N,
                                                              uint32_t* __restrict__ eval, ShardCtl* __restrict__ ctl,
                                                              uint32_t raise_err, uint32_t* __restrict__ lit_bits,
-                                                             uint32_t* __restrict__ pend_apply) {
+                                                             uint32_t* __restrict__ pend_apply, uint32_t inc_direct,
+                                                             uint32_t set_tick, uint32_t tick_base, int32_t dopamine) {
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[ITEMS][8];
   const uint32_t i0 = blockIdx.x * (256u * ITEMS) + threadIdx.x;
@@ -1458,12 +1515,17 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
     if (i < N) tm[r] = timers[i];
   }
   const uint32_t seg_max = ctl->seg_max, pmax = ctl->pmax;
-  const bool inc = batch_counts && batch_counts[k] > 0;
+  // network pushes this tick: per-tick calls say so directly, batches by the tick's count
+  const bool inc = inc_direct || (batch_counts && batch_counts[k] > 0);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     ctl->ctr[0] += 1;
     if (raise_err) atomicOr(&ctl->err, raise_err);
     ctl->fix_count = 0;      // the previous tick's fix-up is done
     ctl->fix_overflow = 0;
+    if (set_tick) {          // per-tick calls: the tick number and dopamine the later stages read
+      ctl->tick_base = tick_base;
+      ctl->dopamine = dopamine;
+    }
   }
   const uint32_t hi = min(seg_max, 30u);   // segments 1..hi are the ones the batch's slots use
   const uint32_t need = hi ? (((2u << hi) - 1u) & ~1u) : 0xFFFFFFFFu;
@@ -1531,6 +1593,8 @@ constexpr int kProItems = 1;   // items per thread of k_rows_prologue_plain
 
 cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   if (s.rows && s.rows->N >= N && s.rows->A >= A && (s.rows->fix || !with_fix)) return cudaSuccess;
+  graph_cache_drop(&s);   // captured graphs hold the old buffers' addresses
+  rows_touched(s);
   rows_free(s);
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   size_t off = 0;
@@ -1598,8 +1662,6 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
   return cudaGetLastError();
 }
 
-// One tick of the row engine (batch mode): prologue, update (+GSOP), fix-up, push.
-// ev (optional) gets the stage boundaries 2..5 recorded (GSOP is part of update).
 // Largest fully-lit bitmap the update kernel stages in shared memory (the
 // 1024-thread variant also uses ~3.4 KB of static shared memory).
 static size_t lit_smem_limit() {
@@ -1629,17 +1691,17 @@ static bool rows_lit(uint32_t A) { return (size_t)lit_smem_bytes(A) <= lit_smem_
 // the spikers are listed for launch_rows_gsop.
 template <bool INLINE>
 static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, uint32_t k,
-                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream) {
+                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream, ColWT wt = ColWT{}) {
   RowCache& r = *s.rows;
   const int sms = sm_count();
   if (rows_lit(A))
     k_rows_update<true, INLINE><<<sms, 1024, lit_smem_bytes(A), stream>>>(
         v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
-        r.lfz, r.wcnt);
+        r.lfz, r.wcnt, wt);
   else
     k_rows_update<false, INLINE><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend,
                                                               r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
-                                                              r.lfz, r.wcnt);
+                                                              r.lfz, r.wcnt, wt);
 }
 
 // The GSOP passes over the spikers the tick's update pass listed (32 warps per
@@ -1663,6 +1725,13 @@ static void launch_rows_gsop(const ShardVramPtrs& v, ShardScratch& s, uint32_t A
   }
 }
 
+// One tick of the row engine: prologue, update (+GSOP), fix-up, push.  In a
+// batch (a.batch) the tick number, dopamine and network spike count come from
+// the control block and the soma pushes may be deferred to the next tick's
+// prologue; a per-tick call (cu_step_day_phase) passes them to the prologue,
+// applies its pushes before it returns, and writes GSOP's weight changes
+// through to the columnar blob (its row cache outlives the call).  ev
+// (optional) gets the stage boundaries 2..5 recorded (GSOP is part of update).
 cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
                              cudaEvent_t* ev, bool have_incoming) {
   RowCache& r = *s.rows;
@@ -1672,18 +1741,27 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   uint32_t raise = 0;
   if (bitmask && ((uint64_t)a.virtual_offset + a.num_virtual > A)) raise |= AXC_ERR_VIRTUAL_RANGE;
   const uint32_t G = max(A, N);
+  const bool per_tick = !a.batch;
   if (G)
     k_rows_prologue_plain<kProItems><<<(G + 256 * kProItems - 1) / (256 * kProItems), 256, 0, stream>>>(
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
-        have_incoming ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N, r.eval, s.ctl,
-        raise, r.lit, a.k > 0 ? s.pend : nullptr);
+        (have_incoming && !per_tick) ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N,
+        r.eval, s.ctl, raise, r.lit, (a.k > 0 && !per_tick) ? s.pend : nullptr,
+        (have_incoming && per_tick) ? 1u : 0u, per_tick ? 1u : 0u, a.tick - a.k, (int32_t)a.dopamine);
   if (ev) cudaEventRecord(ev[2], stream);
+  ColWT wt{};
+  if (per_tick) {
+    wt.w = v.dendrite_weights;
+    wt.om = r.omask;
+    wt.cnt = r.cnt;
+    wt.N = N;
+  }
   // stages: ev[2]..ev[3] the update pass with GSOP, ev[3]..ev[4] fix-up and push
-  launch_rows_update<true>(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream);
+  launch_rows_update<true>(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream, wt);
   if (ev) cudaEventRecord(ev[3], stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
-                                            a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0);
+                                            a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0, wt);
   // the soma pushes: by the next tick's prologue within a batch, here on its last tick
   if (!a.defer_push)
     k_rows_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, r.eval, v.soma_flags, N,

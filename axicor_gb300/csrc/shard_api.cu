@@ -9,6 +9,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
 #include <mutex>
 #include <unordered_map>
 
@@ -71,6 +72,10 @@ __global__ void k_init_sentinels(BurstHeads8* heads, uint32_t total) {  // bindi
 
 }  // namespace
 
+size_t state_blob_bytes(uint32_t padded_n) {  // memory.rs:32-54
+  return (size_t)padded_n * (4 + 1 + 4 + 1 + 4) + (size_t)padded_n * AXC_MAX_DENDRITES * (4 + 2 + 1);
+}
+
 ShardScratch* scratch_for(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons,
                           cudaError_t* err) {
   *err = cudaSuccess;
@@ -80,15 +85,41 @@ ShardScratch* scratch_for(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
   auto it = m.find(key);
   if (it != m.end()) {
     ShardScratch* s = it->second;
-    if (s->padded_n >= padded_n && s->total_axons >= total_axons) return s;
+    if (s->padded_n >= padded_n && s->total_axons >= total_axons) {
+      if (s->state_base != vram->soma_voltage) {   // the same heads with another state allocation
+        s->state_base = vram->soma_voltage;
+        s->tick_rows_valid.store(false);
+      }
+      return s;
+    }
     m.erase(it);
     scratch_free(s);
   }
   ShardScratch* s = new ShardScratch();
   *err = scratch_alloc(s, padded_n, total_axons);
   if (*err != cudaSuccess) { delete s; return nullptr; }
+  s->state_base = vram->soma_voltage;
+  s->state_bytes = state_blob_bytes(padded_n);
   m[key] = s;
   return s;
+}
+
+ShardScratch* scratch_find(const ShardVramPtrs* vram) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto& m = registry();
+  auto it = m.find(vram->axon_heads);
+  return it == m.end() ? nullptr : it->second;
+}
+
+void invalidate_overlapping(const void* dst, size_t size) {
+  if (!dst || size == 0) return;
+  const uintptr_t lo = reinterpret_cast<uintptr_t>(dst), hi = lo + size;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& kv : registry()) {
+    ShardScratch* s = kv.second;
+    const uintptr_t b = reinterpret_cast<uintptr_t>(s->state_base);
+    if (b && lo < b + s->state_bytes && b < hi) s->tick_rows_valid.store(false);
+  }
 }
 
 void scratch_release(const void* key) {
@@ -101,20 +132,15 @@ void scratch_release(const void* key) {
   scratch_free(s);
 }
 
-static ShardScratch* scratch_lookup(const ShardVramPtrs* vram) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  auto& m = registry();
-  auto it = m.find(vram->axon_heads);
-  return it == m.end() ? nullptr : it->second;
-}
+static ShardScratch* scratch_lookup(const ShardVramPtrs* vram) { return scratch_find(vram); }
+
+// Kernels of cu_step_day_phase: 1 the neuron-major row engine with a row cache
+// kept across calls (default), 0 the columnar per-tick kernels.
+static std::atomic<int> g_tick_mode{1};
 
 }  // namespace axc
 
 using namespace axc;
-
-static size_t state_blob_bytes(uint32_t padded_n) {  // memory.rs:32-54
-  return (size_t)padded_n * (4 + 1 + 4 + 1 + 4) + (size_t)padded_n * AXC_MAX_DENDRITES * (4 + 2 + 1);
-}
 
 extern "C" {
 
@@ -184,6 +210,7 @@ int32_t cu_upload_state_blob(const ShardVramPtrs* vram, const void* state_blob, 
             state_blob_bytes(s->padded_n));
     return (int32_t)cudaErrorInvalidValue;
   }
+  if (s) rows_touched(*s);
   cudaError_t err = cudaMemcpy(vram->soma_voltage, state_blob, state_size, cudaMemcpyHostToDevice);
   if (err != cudaSuccess)
     fprintf(stderr, "[cu_upload_state_blob] cudaMemcpy failed: %s\n", cudaGetErrorString(err));
@@ -233,6 +260,29 @@ int32_t cu_step_day_phase(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
   cudaError_t err;
   ShardScratch* s = scratch_for(vram, padded_n, total_axons, &err);
   if (!s) return (int32_t)err;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // The row engine keeps its neuron-major copy of the dendrites across calls
+  // (rebuilt when another entry point wrote the shard or the LUT changed) and
+  // writes GSOP's weight changes through to the columnar blob, so the shard's
+  // memory after every call is what the reference leaves.  Without room for the
+  // copy the columnar kernels run the tick.
+  bool rows = g_tick_mode.load() == 1 && padded_n > 0 && total_axons > 0;
+  if (rows && !(s->rows && s->rows->N >= padded_n && s->rows->A >= total_axons)) {
+    if (rows_alloc(*s, padded_n, total_axons) != cudaSuccess) {
+      cudaGetLastError();   // the failed allocation's error is not this tick's
+      rows = false;
+    }
+  }
+  if (rows) {
+    const uint64_t gen = lut_generation();
+    if (!s->tick_rows_valid.load() || s->tick_rows_lut != gen) {
+      err = launch_rows_begin(*vram, *s, padded_n, total_axons, st);
+      if (err != cudaSuccess) return (int32_t)err;
+      s->tick_rows_valid.store(true);
+      s->tick_rows_lut = gen;
+      s->tick_parity = 0;
+    }
+  }
   TickArgs a{};
   a.padded_n = padded_n;
   a.total_axons = total_axons;
@@ -250,7 +300,14 @@ int32_t cu_step_day_phase(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
   a.dopamine = dopamine;
   a.batch = false;
   a.k = 0;
-  return (int32_t)launch_tick(*vram, *s, a, static_cast<cudaStream_t>(stream));
+  if (rows) {
+    a.rows = true;
+    a.k = s->tick_parity;
+    a.defer_push = false;
+    a.fix_cap = s->rows->fix ? fix_capacity() : 0u;   // no list (population rows): the fix-up rescans
+    s->tick_parity ^= 1u;
+  }
+  return (int32_t)launch_tick(*vram, *s, a, st);
 }
 
 int32_t cu_upload_constant_memory(const VariantParameters* lut) {
@@ -279,13 +336,17 @@ void* gpu_host_alloc(size_t size) {
   return p;
 }
 void gpu_host_free(void* p) { cudaFreeHost(p); }
+// Copies into a shard's .state (the Night Phase's sprouting upload,
+// shard_thread.rs:339-350) make its per-tick row cache stale.
 void gpu_memcpy_host_to_device_async(void* dst, const void* src, size_t size, void* stream) {
+  invalidate_overlapping(dst, size);
   cudaMemcpyAsync(dst, src, size, cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream));
 }
 void gpu_memcpy_device_to_host_async(void* dst, const void* src, size_t size, void* stream) {
   cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream));
 }
 bool gpu_memcpy_host_to_device(void* dst, const void* src, size_t size) {
+  invalidate_overlapping(dst, size);
   cudaError_t err = cudaMemcpy(dst, src, size, cudaMemcpyHostToDevice);
   if (err != cudaSuccess)
     fprintf(stderr, "[gpu_memcpy_host_to_device] %s (size %zu)\n", cudaGetErrorString(err), size);
@@ -354,6 +415,18 @@ int32_t cu_dma_d2h_io(uint8_t* h_output_history, const uint8_t* d_output_history
 }
 
 // ---- engine extras --------------------------------------------------------
+int32_t axc_tick_engine_mode(int32_t mode) {
+  if (mode < 0) return g_tick_mode.load();
+  return g_tick_mode.exchange(mode == 0 ? 0 : 1);
+}
+
+int32_t axc_shard_invalidate(const ShardVramPtrs* vram) {
+  if (!vram) return (int32_t)cudaErrorInvalidValue;
+  ShardScratch* s = scratch_lookup(vram);
+  if (s) rows_touched(*s);
+  return 0;
+}
+
 int32_t axc_shard_error_flags(const ShardVramPtrs* vram, uint32_t clear, uint32_t* out_flags) {
   if (!vram || !out_flags) return (int32_t)cudaErrorInvalidValue;
   ShardScratch* s = scratch_lookup(vram);

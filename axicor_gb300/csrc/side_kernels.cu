@@ -318,6 +318,7 @@ extern "C" {
 
 void launch_sort_and_prune(const ShardVramPtrs* ptrs, uint32_t padded_n, int16_t prune_threshold) {
   if (!ptrs || padded_n == 0) return;
+  if (ShardScratch* s = scratch_find(ptrs)) rows_touched(*s);   // targets and weights move
   k_sort_and_prune<<<(padded_n + kSortNeurons - 1) / kSortNeurons, 256>>>(*ptrs, padded_n, prune_threshold);
 }
 
@@ -435,6 +436,7 @@ void launch_apply_gsop(VramState vram) {
   cudaError_t e;
   ShardScratch* s = scratch_for(&v, vram.padded_n, vram.total_axons, &e);
   if (!s) return;
+  rows_touched(*s);   // columnar weights change
   launch_gsop_stage(v, *s, vram.padded_n, vram.total_axons, 0, nullptr);
 }
 

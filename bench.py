@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--outputs", type=int, default=4096)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-per-tick", action="store_true",
+                    help="skip the per-tick entry point leg (cu_step_day_phase vs the reference's own kernels)")
     ap.add_argument("--engine", default="rows", choices=["rows", "columnar"],
                     help="batch kernels: neuron-major row engine (default) or the per-tick columnar kernels")
     return ap.parse_args()
@@ -347,12 +349,113 @@ def run_gb300(args, dist: Dist) -> dict | None:
                      "evaluated_neurons": int(ctr[5]) / ticks_timed},
         "engine": args.engine,
         "delivered_events_per_s": value_tps * int(ctr[2]) / ticks_timed,
-        "lay": lay, "w": w, "vram": vram,
+        "lay": lay, "w": w, "vram": vram, "eng": eng, "state0": state,
     }
     lib.gpu_free(d_ids)
     lib.gpu_free(d_bm_all)
     lib.gpu_free(d_prof_bm)
     return result
+
+
+def digest(vram) -> str:
+    import hashlib
+    h = hashlib.sha256()
+    h.update(vram.download_state().tobytes())
+    h.update(vram.download_heads().tobytes())
+    return h.hexdigest()
+
+
+def per_tick_leg(r, t0=500, ticks=100, lead=10) -> dict:
+    """cu_step_day_phase, the symbol an unmodified ShardEngine calls once per tick (shard.rs:75-120), on ticks
+    [t0, t0 + ticks) of the brain, against the reference's own GPU Day Phase (physics.cu compiled for sm_103a
+    from the reference sources, launched in cu_step_day_phase's order) on the same ticks from the same state.
+    The brain is brought from its initial state to tick t0 - lead by the batch path; `lead` untimed per-tick
+    calls then precede the timed ticks on both sides (the engine's first call rebuilds its row copy).  CUDA
+    events on each launching stream.  The engine's result is checked against the batch path's over the same
+    ticks (sha256 of state and heads)."""
+    import torch
+    from axicor_gb300 import _native as N
+    from axicor_gb300 import shard as S
+    from oracle import refgpu   # the reference's own kernels, timed as a baseline only
+
+    lib = N.lib()
+    w, lay, vram, eng = r["w"], r["lay"], r["vram"], r["eng"]
+    Np, A = lay.padded_n, lay.total_axons
+    words = (w.num_inputs + 31) // 32
+    start = t0 - lead
+    bm = S.input_bitmask(w.seed, 0, t0 + ticks, w.num_inputs, w.rate_q32)
+    d_bm = S.device_array(bm)
+    io = S.IoDeviceBuffers(words, 0, 0, 100)
+    try:
+        vram.upload_state(r["state0"])
+        vram.upload_axon_heads(np.full(A * 8, 0x80000000, np.uint32))
+        t = 0
+        while t < start:
+            b = min(100, start - t)
+            eng.step_day_phase_batch(b, io, bm[t * words:(t + b) * words], None, None, lay.virtual_offset,
+                                     w.num_inputs, None, w.v_seg, w.dopamine, t)
+            t += b
+        eng.synchronize()
+        snap_s, snap_h = vram.download_state(), vram.download_heads()
+        stream = torch.cuda.ExternalStream(eng.stream)
+
+        def engine_ticks(a, b):
+            for k in range(a, b):
+                err = lib.cu_step_day_phase(C.byref(vram.ptrs), Np, A, w.v_seg, k, d_bm + k * words * 4,
+                                            lay.virtual_offset, w.num_inputs, None, 0, None, None, 0, w.dopamine,
+                                            eng.stream)
+                if err:
+                    raise RuntimeError(f"cu_step_day_phase failed: {err}")
+
+        engine_ticks(start, t0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        engine_ticks(t0, t0 + ticks)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ours_s = e0.elapsed_time(e1) / 1e3
+        d_ours = digest(vram)
+        # the batch path over the same ticks from the same state
+        vram.upload_state(snap_s)
+        vram.upload_axon_heads(snap_h)
+        eng.step_day_phase_batch(lead, io, bm[start * words:t0 * words], None, None, lay.virtual_offset,
+                                 w.num_inputs, None, w.v_seg, w.dopamine, start)
+        eng.step_day_phase_batch(ticks, io, bm[t0 * words:(t0 + ticks) * words], None, None, lay.virtual_offset,
+                                 w.num_inputs, None, w.v_seg, w.dopamine, t0)
+        eng.synchronize()
+        same = digest(vram) == d_ours
+        out = {"ticks": [t0, t0 + ticks], "entry_point": "cu_step_day_phase",
+               "engine_ticks_per_s": ticks / ours_s, "engine_events_per_s": ticks * r["synapses"] / ours_s,
+               "bitexact_vs_batch_path": same}
+        if not refgpu.available():
+            out["reference_kernels"] = "unavailable: reference cubin not built (oracle/build_ref.py needs the sources)"
+            return out
+        vram.upload_state(snap_s)
+        vram.upload_axon_heads(snap_h)
+        rk = refgpu.ReferenceKernels()
+        rk.upload_lut(w.lut)
+        for k in range(start, t0):
+            rk.step(vram, Np, A, w.v_seg, k, d_bm + k * words * 4, lay.virtual_offset, w.num_inputs, None, 0, None,
+                    None, 0, w.dopamine, sync=False)
+        torch.cuda.synchronize()
+        default = torch.cuda.default_stream()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(default)
+        for k in range(t0, t0 + ticks):
+            rk.step(vram, Np, A, w.v_seg, k, d_bm + k * words * 4, lay.virtual_offset, w.num_inputs, None, 0, None,
+                    None, 0, w.dopamine, sync=False)
+        r1.record(default)
+        torch.cuda.synchronize()
+        ref_s = r0.elapsed_time(r1) / 1e3
+        out.update({"reference_kernels_ticks_per_s": ticks / ref_s,
+                    "reference_kernels_events_per_s": ticks * r["synapses"] / ref_s,
+                    "speedup_vs_reference_kernels": ref_s / ours_s,
+                    "reference_kernels": "physics.cu compiled for sm_103a from the reference sources, launched in "
+                                         "cu_step_day_phase's order (physics.cu:441-495), legacy stream"})
+        return out
+    finally:
+        lib.gpu_free(d_bm)
 
 
 def cpu_sample(w, state, heads, lay, tick0, budget_s, threads) -> dict:
@@ -679,6 +782,9 @@ def main():
                    "sample": f"{cs['ticks']} ticks ({cs['seconds']:.1f} s) of the {args.workload} brain from the "
                              f"GPU's state after the timed region; C restatement of physics.cu, OpenMP",
                    "ticks_per_s": cs["ticks_per_s"]}
+        per_tick = None
+        if not args.no_per_tick and dist.world == 1 and args.workload == "plain-1.5M" and args.engine == "rows":
+            per_tick = per_tick_leg(r)
         line = {
             "metric": "synaptic_events_per_s", "value": r["events_per_s"], "unit": "events/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
@@ -703,6 +809,7 @@ def main():
             "per_tick": r["per_tick"],
             "clocks": r["clocks"],
             "cpu_baseline": cpu,
+            "per_tick_entry_point": per_tick,
         }
         print(json.dumps(line), flush=True)
     finally:

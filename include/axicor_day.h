@@ -288,6 +288,24 @@ int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
  * A negative value only queries.  Returns the previous mode. */
 int32_t axc_batch_engine_mode(int32_t mode);
 
+/* Selects the kernels of cu_step_day_phase: 1 (default) the neuron-major row
+ * engine, whose copy of the shard's dendrites (targets and weights by neuron,
+ * the slots whose weights may still move first) lives across calls and whose
+ * GSOP writes every weight it changes through to the .state blob, so that the
+ * shard's memory after each tick is what the reference leaves; 0 the columnar
+ * per-tick kernels.  The copy is rebuilt on the next tick after any entry
+ * point of this library wrote the shard's .state (cu_upload_state_blob,
+ * gpu_memcpy_host_to_device[_async] into it, launch_sort_and_prune,
+ * launch_apply_gsop, the batch, population and learned engines) or uploaded
+ * a LUT.  A negative value only queries.  Returns the previous mode. */
+int32_t axc_tick_engine_mode(int32_t mode);
+
+/* No counterpart in the reference.  A caller that writes a shard's targets,
+ * weights, flags or soma_to_axon by other means than this library (its own
+ * kernels, a raw cudaMemcpy) calls this before the next cu_step_day_phase so
+ * that the per-tick row copy is rebuilt.  Returns 0. */
+int32_t axc_shard_invalidate(const ShardVramPtrs* vram);
+
 /* Capacity of the batch engine's per-tick list of deferred GSOP slots
  * (default and maximum 4,194,304); beyond it the fix-up stage rescans every
  * spiker.  For tests of that path.  Returns the previous capacity. */

@@ -7,9 +7,11 @@ legs of ``bench.py`` use it, as the checker; the engine never calls it.
 
 Pinning: the restatement is checked against every known-answer test the
 reference holds for this path (active-tail predicate, target packing, GSOP
-weight update, homeostasis), in tests/test_oracle_kat.py.  Full-tick parity
-has no reference golden vector (the reference has no test that runs a tick),
-so the tick semantics rest on the line-by-line restatement.
+weight update, homeostasis), in tests/test_oracle_kat.py.  The reference has
+no test that runs a whole tick, so full ticks are pinned against the
+reference's own CUDA kernels, compiled from its sources (build_ref.py) and run
+on the GPU tick by tick from the oracle's state (refgpu.py,
+tests/test_reference_gpu.py).
 """
 from __future__ import annotations
 

@@ -1,11 +1,13 @@
-"""Runs the reference's own Day Phase kernels on the GPU (test infrastructure).
+"""Runs the reference's own Day Phase kernels on the GPU (test and baseline infrastructure).
 
 oracle/build_ref.py compiles genesis-compute/src/cuda/physics.cu into
 oracle/_ref/physics_ref.cubin.  This module loads it with the CUDA driver API
 and launches its kernels in the order and shapes of cu_step_day_phase
 (physics.cu:441-495): 256-thread blocks, reset, inject, spike batch,
 propagate, update, GSOP, readout.  Kernel names are the Itanium-mangled
-names of the reference's kernel signatures.
+names of the reference's kernel signatures.  The tests use it to check the
+oracle against the reference itself; the benchmark times it as the
+reference's own GPU Day Phase beside the engine's per-tick entry point.
 """
 from __future__ import annotations
 
@@ -14,7 +16,7 @@ from pathlib import Path
 
 import numpy as np
 
-CUBIN = Path(__file__).resolve().parents[1] / "oracle" / "_ref" / "physics_ref.cubin"
+CUBIN = Path(__file__).resolve().parent / "_ref" / "physics_ref.cubin"
 
 KERNELS = {
     "reset": "_Z30cu_reset_burst_counters_kernel13ShardVramPtrsj",

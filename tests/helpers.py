@@ -26,7 +26,7 @@ class Twin:
         self.vram = S.VramState(self.N, self.A)
         self.vram.upload_state(state)
         self.vram.upload_axon_heads(heads)
-        self.ids = np.arange(self.N, dtype=np.uint32) if outputs == "all" else outputs
+        self.ids = np.arange(self.N, dtype=np.uint32) if isinstance(outputs, str) and outputs == "all" else outputs
         self.d_ids = S.device_array(self.ids) if self.ids is not None else None
         self.d_out = N.lib().gpu_malloc(max(self.N, 1))
         self.d_bm = N.lib().gpu_malloc(self.words * 4)

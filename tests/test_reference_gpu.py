@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import oracle
-import refgpu
+from oracle import refgpu
 from axicor_gb300 import _native as N
 from axicor_gb300 import shard as S
 from axicor_gb300 import workloads as W
