@@ -83,6 +83,25 @@ class AxcIoBuffers(C.Structure):
     ]
 
 
+class AxcZoneShard(C.Structure):
+    _fields_ = [
+        ("vram", ShardVramPtrs),
+        ("padded_n", C.c_uint32), ("total_axons", C.c_uint32),
+        ("io", AxcIoBuffers),
+        ("h_input_bitmask", C.c_void_p), ("h_incoming_spikes", C.c_void_p), ("h_spike_counts", C.c_void_p),
+        ("virtual_offset", C.c_uint32), ("num_virtual_axons", C.c_uint32),
+        ("mapped_soma_ids_device", C.c_void_p), ("v_seg", C.c_uint32), ("dopamine", C.c_int16),
+        ("h_output_history", C.c_void_p),
+    ]
+
+
+class AxcGhostRoute(C.Structure):
+    _fields_ = [
+        ("src_shard", C.c_uint32), ("dst_shard", C.c_uint32),
+        ("d_src_indices", C.c_void_p), ("d_dst_indices", C.c_void_p), ("count", C.c_uint32),
+    ]
+
+
 class AxcPopBrainDesc(C.Structure):
     _fields_ = [
         ("vram", ShardVramPtrs),
@@ -181,8 +200,15 @@ SIGNATURES: dict[str, tuple] = {
     "axc_tick_engine_mode": (I32, [I32]),
     "axc_shard_invalidate": (I32, [PV]),
     "axc_row_engine_fix_capacity": (U32, [U32]),
+    "axc_row_engine_wait_limit": (U32, [U32]),
     "axc_extract_outgoing_spikes_noalloc": (I32, [P, P, P, U32, U32, U32, P, P, P]),
     "axc_population_create": (I32, [P, U32, C.POINTER(P)]),
+    "axc_step_zone_batch": (I32, [C.POINTER(AxcZoneShard), U32, C.POINTER(AxcGhostRoute), U32, U32, U32, P]),
+    "axc_io_pipeline_create": (I32, [PV, U32, U32, U32, U32, U32, P, U32, U32, U32, C.POINTER(P)]),
+    "axc_io_pipeline_submit": (I32, [P, P, I16, U32, P]),
+    "axc_io_pipeline_outputs": (I32, [P, U32, C.POINTER(P)]),
+    "axc_io_pipeline_wait_input": (I32, [P]),
+    "axc_io_pipeline_destroy": (None, [P]),
     "axc_population_run": (I32, [P, U32, U32, U32, P]),
     "axc_population_tune": (I32, [P, U32, U32, P, P, C.POINTER(C.c_float), U32]),
     "axc_population_set_schedule": (I32, [P, P]),

@@ -44,6 +44,9 @@ struct ShardCtl {
   uint32_t pmax;          // row engine: largest signal_propagation_length of the LUT (batch start)
   uint32_t pad2;
   unsigned long long ctr[8];  // statistics, see axc_shard_counters
+  uint32_t dense[2];      // row engine: tick k (slot k & 1) has an axon off the lit set the row layout assumed
+  unsigned long long pfx_total;   // row engine: slots outside the frozen lit-sum part of the rows (batch start)
+  unsigned long long slot_total;  // row engine: live slots of the rows (batch start)
 };
 
 // Neuron-major copy of the dendrites used by the batch engine for the length
@@ -65,6 +68,8 @@ struct RowCache {
   uint8_t* lfz = nullptr;   // [N] number of those slots (set at batch start)
   uint4* omask = nullptr;   // [N] columnar slots placed first in the row (the movable ones; all when unpermuted)
   uint32_t* wcnt = nullptr; // [2][kMaxUpdateWarps] spikers each warp of the update pass listed (gs_n, gd_n)
+  int2* lsum = nullptr;     // [N] x: wrapping sum of the row's lit-sum weights, y: row positions before them
+  uint32_t* xlit = nullptr; // [A/32+1] axons taken as fully lit when the row layout was made
 };
 
 // Per-shard scratch owned by the engine, next to the reference-visible
@@ -90,6 +95,7 @@ struct ShardScratch {
   std::atomic<bool> tick_rows_valid{false};
   uint64_t tick_rows_lut = 0;           // LUT generation the per-tick row cache was built with
   uint32_t tick_parity = 0;             // per-tick calls alternate the row engine's list slots
+  uint32_t tick_since_build = 0;        // per-tick calls since the row copy was laid out
   const void* state_base = nullptr;     // the shard's .state allocation (invalidation by address)
   size_t state_bytes = 0;
 };
@@ -105,6 +111,8 @@ void rows_free(ShardScratch& s);
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
                               bool row_sum = false, bool permute = true);
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream);
+// Tries of the update pass's first wait for its staged bitmap; returns the previous value.
+uint32_t set_first_wait_limit(uint32_t tries);
 
 // Registry keyed by the axon_heads pointer.  Created by cu_allocate_shard;
 // created lazily (and sized) for shards whose memory the caller allocated.
@@ -150,6 +158,24 @@ constexpr int kTickStages = 5;
 cudaError_t launch_tick(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
                         cudaEvent_t* ev = nullptr);
 cudaError_t launch_reset_burst(const ShardVramPtrs& v, uint32_t padded_n, cudaStream_t stream);
+
+// One shard's batch: the arguments of axc_step_day_phase_batch (batch_engine.cu).
+struct BatchArgs {
+  const ShardVramPtrs* vram;
+  uint32_t padded_n, total_axons, ticks;
+  const AxcIoBuffers* io;
+  const uint32_t *h_bm, *h_in, *h_counts;
+  uint32_t voff, nv;
+  const uint32_t* ids;
+  uint32_t v_seg;
+  int16_t dopamine;
+  uint32_t tick_base;
+};
+cudaError_t batch_prepare(const BatchArgs& b, ShardScratch** out_s, uint32_t* out_rows, cudaStream_t stream);
+cudaError_t batch_capture(const BatchArgs& b, ShardScratch& s, uint32_t rows, uint32_t fix_cap, cudaStream_t cap);
+// dst[dst_indices[i]] = src[src_indices[i]] for src_indices[i] < 2^31 (side_kernels.cu, bindings.cu:341-368).
+cudaError_t ghost_sync(const BurstHeads8* src_heads, BurstHeads8* dst_heads, const uint32_t* src_indices,
+                       const uint32_t* dst_indices, uint32_t count, cudaStream_t stream);
 cudaError_t launch_spike_list_sorted(const ShardVramPtrs& v, uint32_t padded_n, uint32_t* out_ids,
                                      uint32_t* out_count, cudaStream_t stream);
 

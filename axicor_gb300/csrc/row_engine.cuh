@@ -137,6 +137,15 @@ __device__ __forceinline__ void col_write(const ColWT& wt, uint32_t n, uint32_t 
   wt.w[(size_t)q * wt.N + n] = w;
 }
 
+// The lit-sum form runs tick k when the rows' tested prefixes are short (at most
+// an eighth of the live slots: otherwise the 8-lane pass is faster) and every
+// axon the row layout took as fully lit is fully lit this tick.
+__device__ __forceinline__ bool lsum_tick(const ShardCtl* ctl, uint32_t k) {
+  const unsigned long long p = *(volatile const unsigned long long*)&ctl->pfx_total;
+  const unsigned long long c = *(volatile const unsigned long long*)&ctl->slot_total;
+  return c > 0 && p * 8ull <= c && *(volatile const uint32_t*)&ctl->dense[k & 1] == 0u;
+}
+
 // Per-neuron GSOP constants (physics.cu:290-345).
 struct GsopConsts {
   int32_t bm, raw_pot, final_dep;
@@ -277,29 +286,41 @@ __device__ __forceinline__ uint32_t row_pos(uint32_t word, uint32_t lane, uint32
 
 // One neuron's row of the row copy, by one warp, from the columns staged in
 // shared memory (column j, c used slots): invalid targets redirected, movable
-// marks, placement (with permute the movable slots first, then the others,
-// each group in slot order), and the neuron's cnt / amask / omask / lfz.
-// Returns, in every lane, the row's largest segment and (want_sum) its
-// targets checksum.
+// marks, placement, and the neuron's cnt / amask / omask / lfz.
+// Placement with permute: the movable slots first, then (with xlit) the other
+// slots the update pass must test each tick, then the lit-sum slots, each
+// group in slot order; without permute every slot keeps its position.
+// A lit-sum slot (xlit given, permute) is frozen (GSOP cannot move its weight),
+// has a segment in 1..30, belongs to a neuron whose variant length is the LUT
+// maximum, and targets an axon that xlit marks as fully lit: while that axon
+// stays fully lit (the prologue checks it every tick) the slot is a hit, so the
+// update pass adds the row's lit-sum weights as one precomputed wrapping sum
+// (lsum[n].x) and tests only the first lsum[n].y positions.
+// Returns, in every lane, the row's largest segment, (want_sum) its targets
+// checksum and its tested-prefix length.
 struct RowBuilt {
   uint32_t smx;
   unsigned long long hsum;
+  uint32_t pfx;
 };
 
 __device__ __forceinline__ RowBuilt build_row(uint32_t (*s_t)[33], const int16_t (*s_w)[34], uint32_t j, uint32_t n,
                                               uint32_t c, int32_t fz, uint32_t A, bool want_sum, bool permute,
                                               uint32_t* __restrict__ rt, int16_t* __restrict__ rw,
                                               uint16_t* __restrict__ cnt, uint4* __restrict__ amask,
-                                              uint4* __restrict__ omask, uint8_t* __restrict__ lfz) {
+                                              uint4* __restrict__ omask, uint8_t* __restrict__ lfz,
+                                              const uint32_t* __restrict__ xlit = nullptr, bool exact_var = false,
+                                              int2* __restrict__ lsum = nullptr) {
   const uint32_t lane = threadIdx.x & 31;
+  const bool lsum_on = permute && xlit != nullptr && exact_var;
   bool bad = false;
-  uint32_t smx = 0;
+  uint32_t smx = 0, rsum = 0;
   unsigned long long hsum = 0;
-  uint32_t mv[4], all[4];   // movable / used slots, by columnar position
+  uint32_t mv[4], rs[4], all[4];   // movable / lit-sum / used slots, by columnar position
 #pragma unroll
   for (int ch = 0; ch < 4; ch++) {
     const uint32_t q = 32u * ch + lane;
-    bool mov = false;
+    bool mov = false, rest = false;
     if (q < c) {
       uint32_t t = s_t[q][j];
       // an invalid axon id (field 0 or >= A) points at the dummy mask entry A,
@@ -309,32 +330,52 @@ __device__ __forceinline__ RowBuilt build_row(uint32_t (*s_t)[33], const int16_t
         s_t[q][j] = t;
         bad = true;
       }
-      smx = max(smx, t >> AXC_TARGET_SEG_SHIFT);
+      const uint32_t seg = t >> AXC_TARGET_SEG_SHIFT;
+      smx = max(smx, seg);
       if (want_sum) hsum += slot_mix(t, n * kRowStride + q);
       mov = !frozen_weight(s_w[q][j], fz);
+      if (lsum_on && !mov && seg - 1u < 30u) {
+        const uint32_t a = (t & AXC_TARGET_AXON_MASK) - 1u;
+        rest = a < A && ((__ldg(xlit + (a >> 5)) >> (a & 31u)) & 1u);
+      }
+      if (rest) rsum += (uint32_t)(int32_t)s_w[q][j];
     }
     mv[ch] = __ballot_sync(kFull, mov);
+    rs[ch] = __ballot_sync(kFull, rest);
     all[ch] = __ballot_sync(kFull, q < c);
   }
   bad = __any_sync(kFull, bad);
   smx = __reduce_max_sync(kFull, smx);
   if (want_sum) hsum = warp_sum(hsum);
+  rsum = warp_sum(rsum);
   if (bad) {
 #pragma unroll
-    for (int ch = 0; ch < 4; ch++) mv[ch] = all[ch];
+    for (int ch = 0; ch < 4; ch++) { mv[ch] = all[ch]; rs[ch] = 0u; }
+    rsum = 0;
   }
   const uint32_t lf = __popc(mv[0]) + __popc(mv[1]) + __popc(mv[2]) + __popc(mv[3]);
-  // placement: the movable slots first (permute), else every used slot (identity)
-  uint32_t o[4];
+  const uint32_t nrs = __popc(rs[0]) + __popc(rs[1]) + __popc(rs[2]) + __popc(rs[3]);
+  const uint32_t pfx = c - nrs;   // row positions the update pass tests: movable, then the others
+  // placement: movable (o), then tested (x), then lit-sum (rs) with permute; else the identity
+  uint32_t o[4], x[4];
 #pragma unroll
-  for (int ch = 0; ch < 4; ch++) o[ch] = permute ? mv[ch] : all[ch];
-  const uint32_t olf = permute ? lf : c;
-  uint32_t pre = 0, am[4];
+  for (int ch = 0; ch < 4; ch++) {
+    o[ch] = permute ? mv[ch] : all[ch];
+    x[ch] = permute ? (all[ch] & ~mv[ch] & ~rs[ch]) : 0u;
+  }
+  uint32_t po = 0, px = 0, pr = 0, am[4];
+  const uint32_t below = (1u << lane) - 1u;
 #pragma unroll
   for (int ch = 0; ch < 4; ch++) {
     const uint32_t q = 32u * ch + lane;
-    const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
-    pre += __popc(o[ch]);
+    const uint32_t bit = 1u << lane;
+    uint32_t pos;
+    if (o[ch] & bit) pos = po + __popc(o[ch] & below);
+    else if (x[ch] & bit) pos = lf + px + __popc(x[ch] & below);
+    else pos = pfx + pr + __popc(rs[ch] & below);
+    po += __popc(o[ch]);
+    px += __popc(x[ch]);
+    pr += __popc(rs[ch]);
     if (q < c) {
       rt[(size_t)n * kRowStride + pos] = s_t[q][j];
       rw[(size_t)n * kRowStride + pos] = s_w[q][j];
@@ -348,41 +389,47 @@ __device__ __forceinline__ RowBuilt build_row(uint32_t (*s_t)[33], const int16_t
     amask[n] = make_uint4(am[0], am[1], am[2], am[3]);
     omask[n] = make_uint4(o[0], o[1], o[2], o[3]);
     lfz[n] = (uint8_t)lf;
+    if (lsum) lsum[n] = make_int2((int32_t)rsum, (int32_t)pfx);
   }
-  return RowBuilt{smx, hsum};
+  return RowBuilt{smx, hsum, pfx};
 }
 
 // Batch end, 32 neurons from n0 by a 256-thread block: weights rows -> columnar
-// for the slots before the first empty target (slot q of neuron n from row
-// position row_pos of its omask).
+// for the slots of omask (the first group of the row, in slot order).  Those
+// are the only slots whose weights GSOP can have changed (the others are frozen
+// or, without permute, omask holds every used slot).
 __device__ __forceinline__ void writeback_tile(int16_t* __restrict__ weights, uint32_t N, uint32_t n0,
                                                const int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
                                                const uint4* __restrict__ omask, int16_t (*s_w)[34],
                                                uint32_t* s_c) {
+  __shared__ uint4 s_om[32];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint32_t j = warp; j < 32; j += 8) {
     const uint32_t n = n0 + j;
     const uint32_t c = n < N ? (cnt[n] & 0xFFu) : 0u;
-    if (lane == 0) s_c[j] = c;
-    if (c == 0) continue;
-    const uint4 om = omask[n];
+    const uint4 om = c ? omask[n] : make_uint4(0, 0, 0, 0);
+    if (lane == 0) {
+      s_c[j] = (om.x | om.y | om.z | om.w) ? c : 0u;
+      s_om[j] = om;
+    }
     const uint32_t o[4] = {om.x, om.y, om.z, om.w};
-    const uint32_t olf = __popc(om.x) + __popc(om.y) + __popc(om.z) + __popc(om.w);
     uint32_t pre = 0;
 #pragma unroll
     for (int ch = 0; ch < 4; ch++) {
       const uint32_t q = 32u * ch + lane;
-      const uint32_t pos = row_pos(o[ch], lane, q, pre, olf);
+      if (q < c && ((o[ch] >> lane) & 1u))
+        s_w[q][j] = rw[(size_t)n * kRowStride + pre + __popc(o[ch] & ((1u << lane) - 1u))];
       pre += __popc(o[ch]);
-      if (q < c) s_w[q][j] = rw[(size_t)n * kRowStride + pos];
     }
   }
   __syncthreads();
   uint32_t cmax = 0;
   for (int j = 0; j < 32; j++) cmax = max(cmax, s_c[j]);
   const uint32_t c_mine = s_c[lane];
+  const uint4 om = s_om[lane];
+  const uint32_t o[4] = {om.x, om.y, om.z, om.w};
   for (uint32_t r = warp; r < cmax; r += 8)
-    if (r < c_mine) weights[(size_t)r * N + n0 + lane] = s_w[r][lane];
+    if (r < c_mine && ((o[r >> 5] >> (r & 31u)) & 1u)) weights[(size_t)r * N + n0 + lane] = s_w[r][lane];
 }
 
 // Batch start: columnar -> rows.  32 neurons per 256-thread block; the
@@ -403,13 +450,16 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
                                                     uint16_t* __restrict__ cnt, uint4* __restrict__ amask,
                                                     uint4* __restrict__ omask, uint8_t* __restrict__ lfz,
                                                     ShardCtl* __restrict__ ctl, uint32_t A, uint32_t want_sum,
-                                                    uint32_t permute) {
+                                                    uint32_t permute, const uint32_t* __restrict__ xlit,
+                                                    int2* __restrict__ lsum) {
   __shared__ uint32_t s_t[AXC_MAX_DENDRITES][33];
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_cnt[32];
+  __shared__ uint32_t s_pmax;
   const uint32_t n0 = blockIdx.x * 32;
   const uint32_t col = threadIdx.x & 31, r0 = threadIdx.x >> 5;
   if (threadIdx.x < 32) s_cnt[threadIdx.x] = AXC_MAX_DENDRITES;
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
   __syncthreads();
   for (uint32_t ch = 0; ch < AXC_MAX_DENDRITES / 8; ch++) {
     const uint32_t r = ch * 8 + r0, n = n0 + col;
@@ -427,33 +477,44 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     if (__syncthreads_and(mine)) break;
   }
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // the block's longest row, largest segment and (when asked) targets checksum,
-  // one atomic each per block
-  __shared__ uint32_t s_bc[8], s_bs[8];
+  // the block's longest row, largest segment, tested and live slots and (when
+  // asked) targets checksum, one atomic each per block
+  __shared__ uint32_t s_bc[8], s_bs[8], s_bp[8], s_bl[8];
   __shared__ unsigned long long s_bh[8];
-  uint32_t wc = 0, ws = 0;
+  uint32_t wc = 0, ws = 0, wp = 0, wl = 0;
   unsigned long long wh = 0;
   for (uint32_t j = warp; j < 32; j += 8) {
     const uint32_t n = n0 + j;
     if (n >= N) continue;
     const uint32_t c = s_cnt[j];
-    const RowBuilt rb = build_row(s_t, s_w, j, n, c, frozen_from(VARIANT_LUT[flags[n] >> 4]), A, want_sum != 0u,
-                                  permute != 0u, rt, rw, cnt, amask, omask, lfz);
+    const VariantParameters& vp = VARIANT_LUT[flags[n] >> 4];
+    const RowBuilt rb = build_row(s_t, s_w, j, n, c, frozen_from(vp), A, want_sum != 0u, permute != 0u, rt, rw, cnt,
+                                  amask, omask, lfz, xlit, vp.signal_propagation_length == s_pmax, lsum);
     if (lane == 0 && c) {
       wc = max(wc, c);
       ws = max(ws, rb.smx);
       wh += rb.hsum + slot_mix(c, n);
+      wp += rb.pfx;
+      wl += c;
     }
   }
-  if (lane == 0) { s_bc[warp] = wc; s_bs[warp] = ws; s_bh[warp] = wh; }
+  if (lane == 0) { s_bc[warp] = wc; s_bs[warp] = ws; s_bh[warp] = wh; s_bp[warp] = wp; s_bl[warp] = wl; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t bc = 0, bs = 0;
+    uint32_t bc = 0, bs = 0, bp = 0, bl = 0;
     unsigned long long bh = 0;
-    for (int q = 0; q < 8; q++) { bc = max(bc, s_bc[q]); bs = max(bs, s_bs[q]); bh += s_bh[q]; }
+    for (int q = 0; q < 8; q++) {
+      bc = max(bc, s_bc[q]);
+      bs = max(bs, s_bs[q]);
+      bh += s_bh[q];
+      bp += s_bp[q];
+      bl += s_bl[q];
+    }
     if (bc > *(volatile uint32_t*)&ctl->row_smax) atomicMax(&ctl->row_smax, bc);
     if (bs > *(volatile uint32_t*)&ctl->seg_max) atomicMax(&ctl->seg_max, bs);
     if (want_sum) atomicAdd(&ctl->row_sum, bh);
+    if (bp) atomicAdd(&ctl->pfx_total, (unsigned long long)bp);
+    if (bl) atomicAdd(&ctl->slot_total, (unsigned long long)bl);
   }
 }
 
@@ -467,6 +528,8 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
     ctl->seg_max = 0;
     ctl->row_sum = 0;
     ctl->pmax = lut_pmax();
+    ctl->pfx_total = 0;
+    ctl->slot_total = 0;
   }
   if (n >= N) return;
   const uint32_t a = s2a[n];
@@ -754,10 +817,14 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Waits for phase `parity` of bar at most kWaitLimit tries; false: gave up.
+// Waits for phase `parity` of bar at most `tries` tries (default kWaitLimit); false: gave up.
 constexpr uint32_t kWaitLimit = 1u << 16;
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kWaitLimit; it++)
+// Tries of the update pass's first wait for the staged bitmap
+// (axc_row_engine_wait_limit; tests set 0 to take the give-up path).  The
+// drain wait before the block exits always has kWaitLimit tries.
+__device__ uint32_t g_first_wait_limit = kWaitLimit;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t tries = kWaitLimit) {
+  for (uint32_t it = 0; it < tries; it++)
     if (mbar_test(bar, parity)) return true;
   return false;
 }
@@ -907,6 +974,7 @@ __device__ __forceinline__ GlifOut glif_step(const VariantParameters& p, int32_t
 // from the gtab deltas, slow ones on the exact path or deferred to the fix-up
 // list.  Writes the changed weights back to the row (rt_n / rw_n: the
 // neuron's row); returns the slots done.
+template <bool WT = false>
 __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint32_t slowb,
                                              uint32_t c, uint32_t g8, RowShape sh, const int2 (*gtab)[16],
                                              uint32_t var, const uint32_t* rt_n, int16_t* rw_n,
@@ -952,7 +1020,7 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
     }
     if (wj.x != W[j].x || wj.y != W[j].y) {
       *reinterpret_cast<uint2*>(rw_n + q0) = wj;
-      if (wt.w) {
+      if (WT) {
 #pragma unroll
         for (int i = 0; i < 4; i++)
           if (half_of(wj, i) != half_of(W[j], i)) col_write(wt, n, q0 + i, half_of(wj, i));
@@ -990,7 +1058,7 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
       }
       if (nw != w16) {
         rw_n[q] = nw;
-        if (wt.w) col_write(wt, n, q, nw);
+        if (WT) col_write(wt, n, q, nw);
       }
     }
   }
@@ -1003,7 +1071,8 @@ __device__ __forceinline__ uint32_t row_gsop(uint2 (&W)[4], uint32_t hitb, uint3
 // INLINE (rows with their movable slots first): GSOP of each spiker's movable
 // slots on the weights still in registers; else the spikers with movable
 // slots are listed for k_rows_gsop / k_rows_gsop_rows.
-template <bool LIT, bool INLINE>
+// WT: write GSOP's changes through to the columnar blob (the per-tick entry point).
+template <bool LIT, bool INLINE, bool WT = false>
 __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
     k_rows_update(ShardVramPtrs P, uint32_t N, uint32_t A, const uint32_t* __restrict__ rt,
                   int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt, const uint2* __restrict__ mask2,
@@ -1017,6 +1086,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   __shared__ uint64_t s_bar;
   extern __shared__ __align__(128) uint32_t s_lit[];
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
+  if (INLINE && lsum_tick(ctl, k)) return;              // k_rows_update_lsum runs this tick
   if (LIT && threadIdx.x == 0) mbar_init(&s_bar, 1);
   lut_to_smem(lut);
   if (threadIdx.x == 0) s_pmax = lut_pmax();
@@ -1043,7 +1113,7 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   uint32_t wc = 0, wd = 0;   // spikers this warp listed for the GSOP passes
   bool lit_on = true;
   if (LIT) {
-    lit_on = mbar_wait_bounded(&s_bar, 0);
+    lit_on = mbar_wait_bounded(&s_bar, 0, g_first_wait_limit);
     if (!lit_on) err |= AXC_ERR_WAIT_LIMIT;   // then without the shortcut (results exact)
   }
   for (uint32_t base = beg; base < end; base += 32) {
@@ -1104,8 +1174,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
         // GSOP (physics.cu:281-373) of the spiker's movable slots, the first lf
         // of its row; frozen slots (GSOP leaves them as they are) are counted
         if (spike && lf > 0u)
-          gdone += row_gsop(W, hitb, slowb, lf, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p, flags,
-                            dopamine, ctl, fix, fix_cap, n, wt);
+          gdone += row_gsop<WT>(W, hitb, slowb, lf, g8, sh, gtab, var, rt_n, rw_n, P.axon_heads, mask2, A, p,
+                                flags, dopamine, ctl, fix, fix_cap, n, wt);
         if (spike && g8 == 0) gdone += c - lf;
         continue;
       }
@@ -1133,6 +1203,156 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   if (err_any && lane == 0) atomicOr(&ctl->err, err_any);
   block_count(ev_slots, hits, nspk, &ctl->ctr[1]);
   block_count(gdone, nev, 0, &ctl->ctr[4]);
+}
+
+// The hit test of one slot as the 8-lane pass makes it (row_slots): the
+// fully-lit shortcut for segments 1..seg_hi of variants whose length is the LUT
+// maximum (<= 16), else the tick's split masks and, where they do not decide,
+// the eight heads.  *fast: GSOP may take the slot's delta from the gtab table
+// (the hit decides and one same-tick push cannot change it).
+__device__ __forceinline__ bool slot_hit(uint32_t t, bool exact, bool gfast, uint32_t prop, uint32_t seg_hi,
+                                         const uint32_t* __restrict__ lit_bits, const uint2* __restrict__ mask2,
+                                         const BurstHeads8* heads, uint32_t A, bool* fast) {
+  const uint32_t s = t >> AXC_TARGET_SEG_SHIFT;
+  const uint32_t ax = (t & AXC_TARGET_AXON_MASK) - 1u;   // invalid ids were redirected to A (dummy mask entry)
+  if (gfast && (s - 1u) < seg_hi && ((__ldg(lit_bits + (ax >> 5)) >> (ax & 31u)) & 1u)) {
+    *fast = true;
+    return true;
+  }
+  const uint2 m = __ldg(mask2 + ax);
+  const uint32_t sh = min(s, 31u);
+  const uint32_t bx = (m.x >> sh) & 1u, by = (m.y >> sh) & 1u;
+  bool hit = (bx | by) != 0u;
+  if (hit && (s >= 31u || !exact)) hit = hit_exact(heads, A, ax, s, prop);
+  *fast = gfast && s < 31u && !(m.y >> 31) && (bx || by == (s == 0u));
+  return hit;
+}
+
+// ---------------------------------------------------------------------------
+// per tick 2/4, lit-sum form (lsum_tick: short tested prefixes, and every axon
+// the row layout took as fully lit is fully lit): a thread per evaluated
+// neuron.  Its input current is the row's lit-sum (frozen slots on fully-lit
+// axons with segments 1..30: hits whatever the tick, their weights summed once
+// per batch; the dendrite sum is a wrapping i32 sum, so the order cannot change
+// a bit) plus the hits among the first lsum[n].y row positions, tested as the
+// 8-lane pass tests them (physics.cu:182-206); GLIF (physics.cu:209-275); then
+// GSOP of a spiker's movable slots, the first lf positions (physics.cu:281-373),
+// from the gtab deltas, on the exact path or deferred to the fix-up stage.
+// WT: weight changes written through to the columnar blob (per-tick entry point).
+// ---------------------------------------------------------------------------
+constexpr int kLsumBlocks = 5;   // resident 256-thread blocks per SM (48 registers a thread)
+template <bool WT>
+__global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVramPtrs P, uint32_t A, const uint32_t* __restrict__ rt,
+                                                          int16_t* __restrict__ rw, const uint16_t* __restrict__ cnt,
+                                                          const uint2* __restrict__ mask2,
+                                                          const uint32_t* __restrict__ eval, uint32_t* __restrict__ pend,
+                                                          uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
+                                                          uint32_t k, uint32_t fix_cap,
+                                                          const uint32_t* __restrict__ lit_bits,
+                                                          const uint8_t* __restrict__ lfz,
+                                                          const int2* __restrict__ lsum, ColWT wt) {
+  if (!lsum_tick(ctl, k)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ctr[6] += 1;   // ticks on the lit-sum form
+  __shared__ VariantParameters lut[16];
+  __shared__ int2 gtab[16][16];
+  __shared__ uint32_t s_pmax;
+  lut_to_smem(lut);
+  if (threadIdx.x == 0) s_pmax = lut_pmax();
+  __syncthreads();
+  const int32_t dopamine = (int32_t)(int16_t)ctl->dopamine;
+  build_gtab(gtab, lut, dopamine);
+  __syncthreads();
+  const uint32_t tick = ctl->tick_base + k;
+  const uint32_t ecount = ctl->eval_count[k & 1];
+  const uint32_t seg_hi = min(ctl->seg_max, 30u);
+  uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0, tested = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ecount; i += gridDim.x * blockDim.x) {
+    const uint32_t n = eval[i];
+    // every load of the neuron at once
+    const uint8_t flags = P.soma_flags[n];
+    const uint32_t cw = cnt[n];
+    const uint32_t lf = lfz[n];
+    const int2 ls = lsum[n];
+    const int32_t thr0 = P.threshold_offset[n];
+    const int32_t v0 = P.soma_voltage[n];
+    const uint32_t my_axon = P.soma_to_axon[n];
+    const uint32_t c = cw & 0xFFu, pfx = (uint32_t)ls.y;
+    const uint32_t var = flags >> 4;
+    const VariantParameters& p = lut[var];
+    const uint32_t prop = p.signal_propagation_length;
+    const bool exact = prop == s_pmax;
+    const bool gfast = exact && prop <= 16u;
+    if (cw & kRowBad) err |= AXC_ERR_TARGET_RANGE;
+    const uint32_t* rt_n = rt + (size_t)n * kRowStride;
+    int16_t* rw_n = rw + (size_t)n * kRowStride;
+    int32_t i_in = ls.x;
+    uint32_t h = c - pfx;   // the lit-sum slots are hits
+    for (uint32_t q = 0; q < pfx; q += 4) {
+      const uint4 T4 = *reinterpret_cast<const uint4*>(rt_n + q);
+      const uint2 W4 = *reinterpret_cast<const uint2*>(rw_n + q);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        if (q + j >= pfx) break;
+        bool fast;
+        if (slot_hit(word_of(T4, j), exact, gfast, prop, seg_hi, lit_bits, mask2, P.axon_heads, A, &fast)) {
+          i_in = wadd(i_in, (int32_t)half_of(W4, j));
+          h++;
+        }
+      }
+    }
+    ev_slots += c;
+    hits += h;
+    tested += pfx;
+    nev++;
+    const GlifOut o = glif_step(p, v0, thr0, i_in, tick, n);
+    P.soma_voltage[n] = o.v;
+    P.soma_flags[n] = (uint8_t)((flags & 0xF0) | (o.spike ? 0x05 : 0x00));
+    P.threshold_offset[n] = o.thr;
+    P.timers[n] = o.glif ? p.refractory_period : 0;
+    if (!o.spike) continue;
+    nspk++;
+    if (my_axon != AXC_NO_AXON) {
+      if (my_axon < A) atomicAdd(&pend[my_axon], 1u);
+      else err |= AXC_ERR_SOMA_AXON;
+    }
+    // GSOP (physics.cu:281-373) of the movable slots; the frozen ones are left as they are
+    gdone += c - lf;
+    for (uint32_t q = 0; q < lf; q++) {
+      const uint32_t t = rt_n[q];
+      const int16_t w16 = rw_n[q];
+      bool fast;
+      const bool hit = slot_hit(t, exact, gfast, prop, seg_hi, lit_bits, mask2, P.axon_heads, A, &fast);
+      int16_t nw = w16;
+      if (fast) {
+        const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
+        const int2 e = gtab[var][min((uint32_t)aw >> 11, 15u)];
+        int32_t na = aw + (hit ? e.x : -e.y);
+        na = min(max(na, 0), 32767);
+        nw = (int16_t)(w16 < 0 ? -na : na);
+        gdone++;
+      } else {
+        const int r = gsop_general(P.axon_heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u, t >> AXC_TARGET_SEG_SHIFT,
+                                   p, flags, dopamine, &nw);
+        if (r == 2) continue;
+        gdone++;
+        if (r == 1) {
+          const uint32_t slot = atomicAdd(&ctl->fix_count, 1u);
+          if (slot < fix_cap) fix[slot] = (uint32_t)((size_t)n * kRowStride + q);
+          else ctl->fix_overflow = 1u;
+          continue;
+        }
+      }
+      if (nw != w16) {
+        rw_n[q] = nw;
+        if (WT) col_write(wt, n, q, nw);
+      }
+    }
+  }
+  const uint32_t err_any = __reduce_or_sync(kFull, err);
+  if (err_any && (threadIdx.x & 31) == 0) atomicOr(&ctl->err, err_any);
+  block_count(ev_slots, hits, nspk, &ctl->ctr[1]);
+  block_count(gdone, nev, 0, &ctl->ctr[4]);
+  block_count(tested, 0, 0, &ctl->ctr[7]);
 }
 
 // ---------------------------------------------------------------------------
@@ -1353,7 +1573,10 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
   {
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid == 0) ctl->eval_count[(k + 1) & 1] = 0;   // the next tick's list (last used two ticks ago)
+    if (tid == 0) {
+      ctl->eval_count[(k + 1) & 1] = 0;   // the next tick's list (last used two ticks ago)
+      ctl->dense[(k + 1) & 1] = 0;
+    }
     // readout of the tick (physics.cu:378-395): flags are final once the update pass is done
     uint32_t err = 0;
     for (uint32_t j = tid; j < num_outputs; j += stride) {
@@ -1418,6 +1641,7 @@ __global__ void __launch_bounds__(256) k_rows_push(BurstHeads8* __restrict__ hea
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid == 0) {
     ctl->eval_count[(k + 1) & 1] = 0;
+    ctl->dense[(k + 1) & 1] = 0;
     ctl->fix_count = 0;
     ctl->fix_overflow = 0;
   }
@@ -1453,7 +1677,10 @@ __global__ void k_rows_reset_lists(ShardCtl* ctl) {
   ctl->eval_count[1] = 0;
   ctl->fix_count = 0;
   ctl->fix_overflow = 0;
+  ctl->dense[0] = 0;
+  ctl->dense[1] = 0;
 }
+
 
 // ---------------------------------------------------------------------------
 // per tick 1/4 of the plain engine: k_rows_prologue without the learned
@@ -1487,13 +1714,15 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
                                                              uint32_t* __restrict__ eval, ShardCtl* __restrict__ ctl,
                                                              uint32_t raise_err, uint32_t* __restrict__ lit_bits,
                                                              uint32_t* __restrict__ pend_apply, uint32_t inc_direct,
-                                                             uint32_t set_tick, uint32_t tick_base, int32_t dopamine) {
+                                                             uint32_t set_tick, uint32_t tick_base, int32_t dopamine,
+                                                             const uint32_t* __restrict__ xlit) {
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[ITEMS][8];
   const uint32_t i0 = blockIdx.x * (256u * ITEMS) + threadIdx.x;
-  // all loads first: heads, owners, pending pushes, input bits, timers, constants
+  // all loads first: heads, owners, pending pushes, input bits, timers, constants,
+  // and the axons the row layout took as fully lit (xlit, 32 per warp)
   uint4 hx[ITEMS], hy[ITEMS];
-  uint32_t own[ITEMS], npush[ITEMS];
+  uint32_t own[ITEMS], npush[ITEMS], xw[ITEMS];
   uint8_t tm[ITEMS];
 #pragma unroll
   for (int r = 0; r < ITEMS; r++) {
@@ -1501,6 +1730,7 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
     npush[r] = 0;
     own[r] = 0;
     tm[r] = 0;
+    xw[r] = (xlit && i < A) ? __ldg(xlit + (i >> 5)) : 0u;
     if (i < A) {
       const uint4* p = reinterpret_cast<const uint4*>(heads + i);
       hx[r] = p[0];
@@ -1558,7 +1788,11 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
       lit = (m.x & need) == need && !(m.y >> 31);
     }
     const uint32_t lb = __ballot_sync(kFull, lit);
-    if (lane == 0 && i < A) lit_bits[i >> 5] = lb;
+    if (lane == 0 && i < A) {
+      lit_bits[i >> 5] = lb;
+      // an axon the row layout summed as fully lit is not: this tick takes the full pass
+      if (xw[r] & ~lb) atomicOr(&ctl->dense[k & 1], 1u);
+    }
     bool ev = false;
     if (i < N) {
       if (tm[r] > 0) {                              // physics.cu:168-174 after the burst reset
@@ -1591,6 +1825,13 @@ constexpr int kProItems = 1;   // items per thread of k_rows_prologue_plain
 
 }  // namespace
 
+uint32_t set_first_wait_limit(uint32_t tries) {
+  static uint32_t current = kWaitLimit;
+  const uint32_t prev = current;
+  if (cudaMemcpyToSymbol(g_first_wait_limit, &tries, sizeof(tries)) == cudaSuccess) current = tries;
+  return prev;
+}
+
 cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   if (s.rows && s.rows->N >= N && s.rows->A >= A && (s.rows->fix || !with_fix)) return cudaSuccess;
   graph_cache_drop(&s);   // captured graphs hold the old buffers' addresses
@@ -1612,6 +1853,8 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   const size_t o_lfz = off; off = al(off + (size_t)N + 4);
   const size_t o_om = off; off = al(off + (size_t)N * 16 + 16);
   const size_t o_wcnt = off; off = al(off + (size_t)kMaxUpdateWarps * 8);
+  const size_t o_lsum = off; off = al(off + (size_t)N * 8 + 8);
+  const size_t o_xlit = off; off = al(off + ((size_t)A / 32 + 2) * 4 + 16);
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
   if (e != cudaSuccess) return e;
@@ -1636,6 +1879,8 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   r->lfz = reinterpret_cast<uint8_t*>(b + o_lfz);
   r->omask = reinterpret_cast<uint4*>(b + o_om);
   r->wcnt = reinterpret_cast<uint32_t*>(b + o_wcnt);
+  r->lsum = reinterpret_cast<int2*>(b + o_lsum);
+  r->xlit = reinterpret_cast<uint32_t*>(b + o_xlit);
   s.rows = r;
   return cudaSuccess;
 }
@@ -1653,11 +1898,19 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
   k_rows_reset_lists<<<1, 1, 0, stream>>>(s.ctl);
   cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
   if (e != cudaSuccess) return e;
+  // the lit-sum part of the rows (permuted rows only): the axons fully lit in
+  // the last tick the rows saw (the lit bitmap it left) are taken as lit; the
+  // prologue checks every tick that they still are
+  if (permute) {
+    e = cudaMemcpyAsync(r.xlit, r.lit, ((size_t)A / 32 + 1) * 4, cudaMemcpyDeviceToDevice, stream);
+    if (e != cudaSuccess) return e;
+  }
   if (N) {
     k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
     k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, v.soma_flags, N, r.rt,
                                                     r.rw, r.cnt, r.amask, r.omask, r.lfz, s.ctl, A,
-                                                    row_sum ? 1u : 0u, permute ? 1u : 0u);
+                                                    row_sum ? 1u : 0u, permute ? 1u : 0u,
+                                                    permute ? r.xlit : nullptr, permute ? r.lsum : nullptr);
   }
   return cudaGetLastError();
 }
@@ -1673,7 +1926,9 @@ static size_t lit_smem_limit() {
     if (cudaFuncSetAttribute(k_rows_update<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) !=
             cudaSuccess ||
         cudaFuncSetAttribute(k_rows_update<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) !=
-            cudaSuccess) {
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_rows_update<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)lim) != cudaSuccess) {
       cudaGetLastError();
       lim = 0;
     }
@@ -1694,14 +1949,30 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
                                uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream, ColWT wt = ColWT{}) {
   RowCache& r = *s.rows;
   const int sms = sm_count();
-  if (rows_lit(A))
-    k_rows_update<true, INLINE><<<sms, 1024, lit_smem_bytes(A), stream>>>(
+  const bool lit = rows_lit(A);
+  const dim3 grid(lit ? sms : 4 * sms), block(lit ? 1024 : 256);
+  const size_t smem = lit ? lit_smem_bytes(A) : 0;
+  if constexpr (INLINE) {
+    if (wt.w) {   // the per-tick entry point: weight changes written through
+      if (lit)
+        k_rows_update<true, true, true><<<grid, block, smem, stream>>>(
+            v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n,
+            r.gd_n, r.lfz, r.wcnt, wt);
+      else
+        k_rows_update<false, true, true><<<grid, block, smem, stream>>>(
+            v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n,
+            r.gd_n, r.lfz, r.wcnt, wt);
+      return;
+    }
+  }
+  if (lit)
+    k_rows_update<true, INLINE><<<grid, block, smem, stream>>>(
         v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
         r.lfz, r.wcnt, wt);
   else
-    k_rows_update<false, INLINE><<<4 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend,
-                                                              r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
-                                                              r.lfz, r.wcnt, wt);
+    k_rows_update<false, INLINE><<<grid, block, smem, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend,
+                                                                r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
+                                                                r.lfz, r.wcnt, wt);
 }
 
 // The GSOP passes over the spikers the tick's update pass listed (32 warps per
@@ -1747,7 +2018,7 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
         (have_incoming && !per_tick) ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N,
         r.eval, s.ctl, raise, r.lit, (a.k > 0 && !per_tick) ? s.pend : nullptr,
-        (have_incoming && per_tick) ? 1u : 0u, per_tick ? 1u : 0u, a.tick - a.k, (int32_t)a.dopamine);
+        (have_incoming && per_tick) ? 1u : 0u, per_tick ? 1u : 0u, a.tick - a.k, (int32_t)a.dopamine, r.xlit);
   if (ev) cudaEventRecord(ev[2], stream);
   ColWT wt{};
   if (per_tick) {
@@ -1756,8 +2027,16 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
     wt.cnt = r.cnt;
     wt.N = N;
   }
-  // stages: ev[2]..ev[3] the update pass with GSOP, ev[3]..ev[4] fix-up and push
-  launch_rows_update<true>(v, s, N, A, a.k, min(a.fix_cap, kFixCap), nullptr, stream, wt);
+  // stages: ev[2]..ev[3] the update pass with GSOP, ev[3]..ev[4] fix-up and push.
+  // Both forms are launched; each returns at once on the other's ticks.
+  const uint32_t fix_cap = min(a.fix_cap, kFixCap);
+  launch_rows_update<true>(v, s, N, A, a.k, fix_cap, nullptr, stream, wt);
+  if (per_tick)
+    k_rows_update_lsum<true><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                          s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt);
+  else
+    k_rows_update_lsum<false><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                                                           s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt);
   if (ev) cudaEventRecord(ev[3], stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,

@@ -137,6 +137,10 @@ static ShardScratch* scratch_lookup(const ShardVramPtrs* vram) { return scratch_
 // Kernels of cu_step_day_phase: 1 the neuron-major row engine with a row cache
 // kept across calls (default), 0 the columnar per-tick kernels.
 static std::atomic<int> g_tick_mode{1};
+// Per-tick calls between two layouts of the row copy: a new layout follows the
+// weights that froze and the axons that became fully lit meanwhile (the copy is
+// rebuilt from the .state blob, which the write-through keeps current).
+constexpr uint32_t kTickRelayout = 64;
 
 }  // namespace axc
 
@@ -275,13 +279,15 @@ int32_t cu_step_day_phase(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
   }
   if (rows) {
     const uint64_t gen = lut_generation();
-    if (!s->tick_rows_valid.load() || s->tick_rows_lut != gen) {
+    if (!s->tick_rows_valid.load() || s->tick_rows_lut != gen || s->tick_since_build >= kTickRelayout) {
       err = launch_rows_begin(*vram, *s, padded_n, total_axons, st);
       if (err != cudaSuccess) return (int32_t)err;
       s->tick_rows_valid.store(true);
       s->tick_rows_lut = gen;
       s->tick_parity = 0;
+      s->tick_since_build = 0;
     }
+    s->tick_since_build++;
   }
   TickArgs a{};
   a.padded_n = padded_n;

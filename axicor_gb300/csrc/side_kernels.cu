@@ -295,6 +295,17 @@ cudaError_t noalloc_scratch(uint32_t** out) {
   return cudaSuccess;
 }
 
+}  // namespace
+
+cudaError_t ghost_sync(const BurstHeads8* src_heads, BurstHeads8* dst_heads, const uint32_t* src_indices,
+                       const uint32_t* dst_indices, uint32_t count, cudaStream_t stream) {
+  if (count == 0) return cudaSuccess;
+  return launch_k(k_ghost_sync, dim3((count + 255) / 256), dim3(256), stream, src_heads, dst_heads, src_indices,
+                  dst_indices, count);
+}
+
+namespace {
+
 ShardVramPtrs from_legacy(const VramState& s) {
   ShardVramPtrs v;
   v.soma_voltage = s.voltage;
@@ -324,9 +335,7 @@ void launch_sort_and_prune(const ShardVramPtrs* ptrs, uint32_t padded_n, int16_t
 
 void launch_ghost_sync(const BurstHeads8* src_heads, BurstHeads8* dst_heads, const uint32_t* src_indices,
                        const uint32_t* dst_indices, uint32_t count, void* stream) {
-  if (count == 0) return;
-  k_ghost_sync<<<(count + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(src_heads, dst_heads,
-                                                                                  src_indices, dst_indices, count);
+  ghost_sync(src_heads, dst_heads, src_indices, dst_indices, count, static_cast<cudaStream_t>(stream));
 }
 
 void launch_extract_outgoing_spikes(const BurstHeads8* axon_heads, const uint32_t* src_indices,

@@ -244,6 +244,48 @@ class ShardEngine:
             pass
 
 
+class IoPipeline:
+    """Double-buffered batch I/O of one shard (axc_io_pipeline_*): the device side of the reference's input
+    swapchain (io_server.rs:20-85) and per-batch output download (shard_thread.rs:208-227).  submit() queues a
+    batch and returns at once; outputs(back) waits for the readout of the batch submitted `back` submits ago."""
+
+    def __init__(self, vram: VramState, sync_batch_ticks: int, input_words_per_tick: int, num_outputs: int,
+                 mapped_soma_ids_device: int | None, virtual_offset: int, num_virtual_axons: int, v_seg: int = 1):
+        h = C.c_void_p()
+        N.check(N.lib().axc_io_pipeline_create(C.byref(vram.ptrs), vram.padded_n, vram.total_axons,
+                                               sync_batch_ticks, input_words_per_tick, num_outputs,
+                                               mapped_soma_ids_device, virtual_offset, num_virtual_axons, v_seg,
+                                               C.byref(h)), "axc_io_pipeline_create")
+        self.handle = h.value
+        self.batch, self.num_outputs = sync_batch_ticks, num_outputs if mapped_soma_ids_device else 0
+
+    def submit(self, h_input_bitmask_ptr: int | None, tick_base: int, dopamine: int = 0,
+               stream: int | None = None) -> None:
+        N.check(N.lib().axc_io_pipeline_submit(self.handle, h_input_bitmask_ptr, dopamine, tick_base, stream),
+                "axc_io_pipeline_submit")
+
+    def outputs(self, back: int = 0) -> np.ndarray:
+        p = C.c_void_p()
+        N.check(N.lib().axc_io_pipeline_outputs(self.handle, back, C.byref(p)), "axc_io_pipeline_outputs")
+        n = self.batch * self.num_outputs
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint8)), shape=(n,)).copy() if n else np.zeros(0,
+                                                                                                          np.uint8)
+
+    def wait_input(self) -> None:
+        N.check(N.lib().axc_io_pipeline_wait_input(self.handle), "axc_io_pipeline_wait_input")
+
+    def close(self) -> None:
+        if self.handle:
+            N.lib().axc_io_pipeline_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def device_array(host: np.ndarray) -> int:
     """Copies a host array to a new device buffer (gpu_malloc); returns the device pointer."""
     host = np.ascontiguousarray(host)
@@ -255,5 +297,5 @@ def device_array(host: np.ndarray) -> int:
     return p
 
 
-__all__ = ["VramState", "ShardEngine", "IoDeviceBuffers", "PinnedBuffer", "generate_brain", "input_bitmask",
+__all__ = ["VramState", "ShardEngine", "IoDeviceBuffers", "IoPipeline", "PinnedBuffer", "generate_brain", "input_bitmask",
            "upload_lut", "device_array", "BYTES_PER_NEURON"]

@@ -184,13 +184,18 @@ def update_kernel_bytes(ticks, evaluated, spikes, N):
     return 6 * evaluated + ticks * 20 * N + 4 * spikes
 
 
-def rows_update_kernel_bytes(evaluated_slots, evaluated_neurons, spikes):
-    """Algorithmic bytes of the row engine's update pass (k_rows_update): 6 B per evaluated slot (u32 target +
-    i16 weight read), 24 B per evaluated neuron (flags, slot count, list entry, voltage and threshold read;
-    voltage, flags, threshold, timer written), 4 B per spike (soma_to_axon).  The pass also applies GSOP to the
-    spikers' movable slots, whose weights it already holds; their write-back (a few hundred kB per tick in the
-    steady state) is not counted."""
-    return 6 * evaluated_slots + 24 * evaluated_neurons + 4 * spikes
+def rows_update_kernel_bytes(evaluated_slots, evaluated_neurons, spikes, ticks=1, lit_ticks=0, tested=0):
+    """Bytes the row engine's update stage must move.  On a full-pass tick (k_rows_update): 6 B per evaluated
+    slot (u32 target + i16 weight read), 24 B per evaluated neuron (flags, slot count, list entry, voltage and
+    threshold read; voltage, flags, threshold, timer written), 4 B per spike (soma_to_axon).  On a lit-sum tick
+    (k_rows_update_lsum) the row's frozen slots on fully-lit axons arrive as one 8-byte record (sum, tested
+    length) instead of 6 B a slot: 32 B per evaluated neuron, 6 B per tested slot, 4 B per spike.  GSOP's
+    write-back of the movable weights (a few hundred kB per tick in the steady state) is not counted.  With both
+    forms in the window the per-neuron and per-slot terms are split by the fraction of lit-sum ticks."""
+    f = lit_ticks / ticks if ticks else 0.0
+    full = 6 * evaluated_slots + 24 * evaluated_neurons
+    lit = 32 * evaluated_neurons + 6 * tested / f if f else 0.0
+    return (1 - f) * full + f * lit + 4 * spikes
 
 
 def run_gb300(args, dist: Dist) -> dict | None:
@@ -219,7 +224,7 @@ def run_gb300(args, dist: Dist) -> dict | None:
     d_ids = S.device_array(ids)
     io = S.IoDeviceBuffers(words, 0, n_out, B)
 
-    total_ticks = (Wm + 2 * K) * B
+    total_ticks = (Wm + 2 * K + 2) * B
     bm_all = S.input_bitmask(w.seed, 0, total_ticks, w.num_inputs, w.rate_q32)
     d_bm_all = S.device_array(bm_all)
     tick = 0
@@ -260,10 +265,19 @@ def run_gb300(args, dist: Dist) -> dict | None:
     ticks_timed = K * B
     value_tps = dist.world * ticks_timed / t_max
 
-    # e2e: pinned host inputs and a host read of the readout, through the same call
+    # e2e: pinned host inputs and a host read of every batch's readout, through the double-buffered batch I/O
+    # (axc_io_pipeline_*): each step queues one batch from host memory and reads the previous batch's readout on
+    # the host, so the next upload and the last readout overlap the running batch
     h_bm = S.PinnedBuffer(K * B * words, np.uint32)
     h_bm.array[:] = bm_all[tick * words:(tick + K * B) * words]
-    h_out = S.PinnedBuffer(B * n_out, np.uint8)
+    pipe = S.IoPipeline(vram, B, words, n_out, d_ids, lay.virtual_offset, w.num_inputs, w.v_seg)
+    pipe.submit(h_bm.as_ptr(), tick, w.dopamine, eng.stream)          # warm: both buffer slots' graphs
+    pipe.submit(h_bm.as_ptr() + B * words * 4, tick + B, w.dopamine, eng.stream)
+    pipe.outputs(1)
+    pipe.outputs(0)
+    tick += 2 * B
+    h_bm.array[:] = bm_all[tick * words:(tick + K * B) * words]
+    readout_spikes = 0
     dist.barrier()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -271,24 +285,22 @@ def run_gb300(args, dist: Dist) -> dict | None:
     wall0 = time.perf_counter()
     e0.record(stream)
     for k in range(K):
-        src = h_bm.as_ptr() + k * B * words * 4
-        err = lib.axc_step_day_phase_batch(C.byref(vram.ptrs), lay.padded_n, lay.total_axons, B,
-                                           C.byref(io.as_struct()), src, None, None, lay.virtual_offset,
-                                           w.num_inputs, d_ids, w.v_seg, w.dopamine, tick, h_out.as_ptr(),
-                                           eng.stream)
-        if err:
-            raise RuntimeError(f"axc_step_day_phase_batch (e2e) failed: {err}")
+        pipe.submit(h_bm.as_ptr() + k * B * words * 4, tick, w.dopamine, eng.stream)
+        if k:
+            readout_spikes += int(pipe.outputs(1).sum())
         tick += B
+    readout_spikes += int(pipe.outputs(0).sum())
     e1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
+    pipe.close()
     e2e_s = dist.max(max(e0.elapsed_time(e1) / 1e3, wall))
     e2e_tps = dist.world * K * B / e2e_s
 
     # per-kernel CUDA-event timing on the launching stream (same regime, right after)
     prof_ticks = min(50, B)
     out_ms = (C.c_float * 5)()
-    out_cnt = (C.c_uint64 * 5)()
+    out_cnt = (C.c_uint64 * 7)()
     d_prof_bm = S.device_array(bm_all[:prof_ticks * words])
     err = lib.axc_profile_ticks(C.byref(vram.ptrs), lay.padded_n, lay.total_axons, w.v_seg, tick, prof_ticks,
                                 d_prof_bm, words, lay.virtual_offset, w.num_inputs, w.dopamine, engine, eng.stream,
@@ -304,10 +316,12 @@ def run_gb300(args, dist: Dist) -> dict | None:
         names = ["network_ids", "axons", "update", "push", "gsop"]
         kernels = {"axons": "k_axons", "update": "k_update", "push": "k_push", "gsop": "k_gsop"}
     top = int(np.argmax(stage_ms))
-    ev, hits, spk, gs, nev = (int(x) for x in out_cnt)
+    ev, hits, spk, gs, nev, lit_ticks, tested = (int(x) for x in out_cnt)
+    if engine == 1 and lit_ticks:
+        kernels["update"] = "k_rows_update_lsum" if lit_ticks == prof_ticks else "k_rows_update+k_rows_update_lsum"
     A_ = lay.total_axons
     if engine == 1 and names[top] == "update":
-        kb = rows_update_kernel_bytes(ev, nev, spk)
+        kb = rows_update_kernel_bytes(ev, nev, spk, prof_ticks, lit_ticks, tested)
     elif names[top] == "update":
         kb = update_kernel_bytes(prof_ticks, ev, spk, lay.padded_n)
     elif names[top] == "gsop":
@@ -798,8 +812,10 @@ def main():
                        "engine": r["engine"],
                        "timed_ticks": [args.warmup * args.ticks_per_step,
                                        (args.warmup + args.steps) * args.ticks_per_step],
-                       "e2e_ticks": [(args.warmup + args.steps) * args.ticks_per_step,
-                                     (args.warmup + 2 * args.steps) * args.ticks_per_step]},
+                       "e2e_ticks": [(args.warmup + args.steps + 2) * args.ticks_per_step,
+                                     (args.warmup + 2 * args.steps + 2) * args.ticks_per_step],
+                       "e2e_io": "axc_io_pipeline_*: pinned host bitmask up and readout down every step, "
+                                 "double-buffered against the running batch"},
             "e2e": {"value": r["e2e_events_per_s"], "unit": "events/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ticks_per_s": r["e2e_ticks_per_s"]},
             "gpu_launches": r["launches"],

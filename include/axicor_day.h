@@ -267,6 +267,69 @@ int32_t axc_step_day_phase_batch(const ShardVramPtrs* vram, uint32_t padded_n,
                                  uint32_t v_seg, int16_t dopamine, uint32_t tick_base,
                                  uint8_t* h_output_history, void* stream);
 
+/* Zone batch: one batch of every shard of this GPU with the intra-GPU ghost
+ * sync behind it, as one CUDA graph (captured once per zone shape).  It
+ * equals, bit for bit, the reference node loop's batch
+ * (genesis-node/src/node/mod.rs:330-420): ShardEngine::step_day_phase_batch
+ * on every shard (here each shard's tick loop is a parallel branch of the
+ * graph), the device barrier (mod.rs:388), then launch_ghost_sync for every
+ * route in order (mod.rs:409-411), all before the call's stream moves on.
+ * Each shard entry carries the arguments of axc_step_day_phase_batch; the
+ * ghost routes copy heads src -> dst as launch_ghost_sync does.  A shard may
+ * appear once.  Synchronous only when some shard asks for its output history
+ * (as axc_step_day_phase_batch).  No counterpart call in the reference, which
+ * issues these launches from the node loop one by one. */
+typedef struct AxcZoneShard {
+  ShardVramPtrs vram;
+  uint32_t padded_n, total_axons;
+  AxcIoBuffers io;
+  const uint32_t* h_input_bitmask;    /* [batch][input_words_per_tick] or NULL */
+  const uint32_t* h_incoming_spikes;  /* [batch][max_spikes_per_tick] or NULL */
+  const uint32_t* h_spike_counts;     /* [batch] or NULL */
+  uint32_t virtual_offset, num_virtual_axons;
+  const uint32_t* mapped_soma_ids_device;
+  uint32_t v_seg;
+  int16_t dopamine;
+  uint8_t* h_output_history;          /* num_outputs x batch bytes, or NULL */
+} AxcZoneShard;
+
+typedef struct AxcGhostRoute {
+  uint32_t src_shard, dst_shard;      /* indices into the shard array */
+  const uint32_t* d_src_indices;      /* device [count] */
+  const uint32_t* d_dst_indices;      /* device [count] */
+  uint32_t count;
+} AxcGhostRoute;
+
+int32_t axc_step_zone_batch(const AxcZoneShard* shards, uint32_t nshards, const AxcGhostRoute* routes,
+                            uint32_t nroutes, uint32_t sync_batch_ticks, uint32_t tick_base, void* stream);
+
+/* Double-buffered batch I/O for one shard: the device side of the
+ * reference's input swapchain (genesis-node/src/network/io_server.rs:20-85)
+ * and per-batch output download (genesis-node/src/node/shard_thread.rs:208-227).
+ * The pipeline owns two device input bitmasks ([batch][words] u32), two
+ * device output histories and two pinned host output histories
+ * ([batch][num_outputs] u8), an upload stream and a download stream.
+ * axc_io_pipeline_submit queues one batch and returns at once: the bitmask
+ * goes up on the upload stream (into the buffer batch b - 2 used, once that
+ * batch has read it), the batch runs on `stream` as axc_step_day_phase_batch
+ * once its upload landed, and its output history comes down on the download
+ * stream once it is done.  So the next batch's upload overlaps this batch's
+ * ticks, and this batch's readout overlaps the next batch's ticks.  Pass the
+ * bitmask from pinned memory for the copy to be asynchronous; the host buffer
+ * may be rewritten after axc_io_pipeline_wait_input.  axc_io_pipeline_outputs
+ * waits for the readout of the batch submitted `back` (0 or 1) submits ago and
+ * returns its pinned output history, valid until two submits later.  No
+ * counterpart call in the reference. */
+int32_t axc_io_pipeline_create(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons,
+                               uint32_t sync_batch_ticks, uint32_t input_words_per_tick, uint32_t num_outputs,
+                               const uint32_t* mapped_soma_ids_device, uint32_t virtual_offset,
+                               uint32_t num_virtual_axons, uint32_t v_seg, void** out_handle);
+int32_t axc_io_pipeline_submit(void* handle, const uint32_t* h_input_bitmask, int16_t dopamine,
+                               uint32_t tick_base, void* stream);
+int32_t axc_io_pipeline_outputs(void* handle, uint32_t back, const uint8_t** out_history);
+int32_t axc_io_pipeline_wait_input(void* handle);
+void axc_io_pipeline_destroy(void* handle);
+
 /* Instrumented ticks for measurement: runs `ticks` ticks (tick = tick0 + k,
  * bitmask row k of the device array d_input_bitmask) without a graph, with
  * CUDA events recorded on `stream` around each stage.  engine 0: the
@@ -274,9 +337,10 @@ int32_t axc_step_day_phase_batch(const ShardVramPtrs* vram, uint32_t padded_n,
  * neuron-major kernels (the ticks then form one batch, rows built before and
  * weights written back after).  Sets out_ms[5] to the stage times in
  * milliseconds (network ids, axons, update, push, GSOP; with engine 1 GSOP is
- * part of update and "push" includes the GSOP fix-up) and out_counts[5] to
- * the ticks' totals of evaluated slots, hits, spikes, GSOP slots and
- * evaluated (non-refractory) neurons.  Synchronous. */
+ * part of update and "push" includes the GSOP fix-up) and out_counts[7] to
+ * the ticks' totals of evaluated slots, hits, spikes, GSOP slots, evaluated
+ * (non-refractory) neurons, ticks on the lit-sum form and the slots that form
+ * tested (the counters [1]..[7] of axc_shard_counters).  Synchronous. */
 int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t total_axons,
                           uint32_t v_seg, uint32_t tick0, uint32_t ticks,
                           const uint32_t* d_input_bitmask, uint32_t words_per_tick,
@@ -311,10 +375,21 @@ int32_t axc_shard_invalidate(const ShardVramPtrs* vram);
  * spiker.  For tests of that path.  Returns the previous capacity. */
 uint32_t axc_row_engine_fix_capacity(uint32_t cap);
 
+/* Tries of the update pass's first wait for the fully-lit bitmap it stages
+ * in shared memory (default 65,536).  A wait that runs out sets
+ * AXC_ERR_WAIT_LIMIT and the pass continues without the bitmap (results
+ * unchanged); before its block exits it waits again, always with the full
+ * limit, so that no copy is left in flight.  0 makes every first wait give up
+ * at once: for tests of that path.  Returns the previous value. */
+uint32_t axc_row_engine_wait_limit(uint32_t tries);
+
 /* Per-tick counters accumulated by the device since the last reset:
  *  [0] ticks, [1] evaluated slots (non-refractory neurons, up to first empty),
  *  [2] delivered hits, [3] GLIF+heartbeat spikes, [4] GSOP slots updated,
- *  [5] evaluated (non-refractory) neurons. */
+ *  [5] evaluated (non-refractory) neurons, [6] ticks the row engine ran on
+ *  its lit-sum form (frozen slots on fully-lit axons added as one per-row
+ *  sum; the other ticks scan every slot), [7] slots the lit-sum ticks tested
+ *  one by one. */
 int32_t axc_shard_counters(const ShardVramPtrs* vram, uint32_t reset, uint64_t out[8]);
 
 /* Allocation-free outgoing-spike extraction.  No counterpart in the

@@ -62,6 +62,11 @@ int main(void) {
   P(VariantParameters, d1_affinity) P(VariantParameters, d2_affinity)
   P(ShardVramPtrs, axon_heads) P(AxcBrainSpec, seed) P(AxcIoBuffers, num_outputs)
   P(VramState, voltage) P(VramState, axon_heads) P(VramState, telemetry_spikes)
+  printf("AxcZoneShard %zu %zu\n", sizeof(AxcZoneShard), _Alignof(AxcZoneShard));
+  printf("AxcGhostRoute %zu %zu\n", sizeof(AxcGhostRoute), _Alignof(AxcGhostRoute));
+  P(AxcZoneShard, io) P(AxcZoneShard, h_input_bitmask) P(AxcZoneShard, mapped_soma_ids_device)
+  P(AxcZoneShard, dopamine) P(AxcZoneShard, h_output_history) P(AxcGhostRoute, d_src_indices)
+  P(AxcGhostRoute, count)
   return 0;
 }
 """
@@ -107,6 +112,12 @@ def test_struct_layouts(tmp_path):
     assert C.sizeof(N.AxcBrainLayout) == v["AxcBrainLayout"][0]
     assert C.sizeof(N.AxcIoBuffers) == v["AxcIoBuffers"][0]
     assert N.AxcIoBuffers.num_outputs.offset == v["AxcIoBuffers.num_outputs"][0]
+    assert C.sizeof(N.AxcZoneShard) == v["AxcZoneShard"][0]
+    assert C.sizeof(N.AxcGhostRoute) == v["AxcGhostRoute"][0]
+    for f in ("io", "h_input_bitmask", "mapped_soma_ids_device", "dopamine", "h_output_history"):
+        assert getattr(N.AxcZoneShard, f).offset == v[f"AxcZoneShard.{f}"][0], f
+    for f in ("d_src_indices", "count"):
+        assert getattr(N.AxcGhostRoute, f).offset == v[f"AxcGhostRoute.{f}"][0], f
 
 
 def test_variant_dtype_roundtrip():

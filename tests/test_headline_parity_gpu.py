@@ -184,7 +184,7 @@ def _digest(vram):
 def test_learned_forced_sparse_on_quiet_1_5m_matches_plain(gpu):
     """The learned engine with every tick on the sparse form (the spikers of the sparse GLIF pass go to the
     GSOP passes after it) against the plain batch path: 300 ticks of the quiet 1.5M brain, sha256 of the
-    final state and heads."""
+    final state and heads, and both against the oracle."""
     ticks = 300
     w = W.homeostatic(W.config1(ticks=ticks))
     lay, state, heads = S.generate_brain(w.spec())
@@ -198,7 +198,8 @@ def test_learned_forced_sparse_on_quiet_1_5m_matches_plain(gpu):
     learned = S.VramState(lay.padded_n, lay.total_axons)
     learned.upload_state(state)
     learned.upload_axon_heads(heads)
-    del state, heads
+    oracle.run_ticks(state, heads, w.lut, lay.padded_n, lay.total_axons, w.v_seg, 0, ticks, bm, words,
+                     lay.virtual_offset, w.num_inputs)
     eng = S.ShardEngine(plain)
     io = S.IoDeviceBuffers(words, 0, 0, 100)
     le = L.LearnedEngine(learned, lay.padded_n, lay.total_axons, lay.virtual_offset, w.num_inputs, d_bm, words,
@@ -210,6 +211,10 @@ def test_learned_forced_sparse_on_quiet_1_5m_matches_plain(gpu):
         N.lib().gpu_device_synchronize()
         st = le.stats()
         assert st["sparse_ticks"] + st["overflow_reruns"] == ticks and st["sparse_ticks"] > ticks // 2, st
+        for name, v in (("plain", plain), ("learned", learned)):
+            gs, gh = v.download_state(), v.download_heads()
+            same = np.array_equal(gs, state) and np.array_equal(gh, heads)
+            assert same, f"{name} differs from the oracle after {ticks} ticks: {_state_diff(gs, state, lay.padded_n)}"
         assert _digest(learned) == _digest(plain)
     finally:
         le.close()
