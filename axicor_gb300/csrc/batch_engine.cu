@@ -49,7 +49,7 @@ __global__ void k_set_batch_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopam
   ctl->dopamine = dopamine;
 }
 
-cudaError_t ensure_counts(ShardScratch& s, uint32_t batch, bool* realloc) {
+cudaError_t ensure_counts(ShardScratch& s, uint32_t batch, bool* realloc, cudaStream_t stream) {
   if (s.batch_cap >= batch && s.batch_counts) return cudaSuccess;
   *realloc = true;
   if (s.batch_counts) cudaFree(s.batch_counts);
@@ -58,7 +58,7 @@ cudaError_t ensure_counts(ShardScratch& s, uint32_t batch, bool* realloc) {
   cudaError_t e = cudaMalloc(&s.batch_counts, (size_t)batch * 4);
   if (e != cudaSuccess) return e;
   s.batch_cap = batch;
-  return cudaMemset(s.batch_counts, 0, (size_t)batch * 4);
+  return cudaMemsetAsync(s.batch_counts, 0, (size_t)batch * 4, stream);   // in the caller's stream order
 }
 
 }  // namespace
@@ -113,12 +113,12 @@ cudaError_t batch_prepare(const BatchArgs& b, ShardScratch** out_s, uint32_t* ou
   // Captured graphs hold the addresses of the scratch buffers: any
   // reallocation below drops them.
   bool realloc = false;
-  e = ensure_counts(*s, b.ticks, &realloc);
+  e = ensure_counts(*s, b.ticks, &realloc, stream);
   if (e != cudaSuccess) return e;
   const uint32_t rows = g_batch_mode.load() == 1 ? 1u : 0u;
   if (rows) {
     const void* before = s->rows ? s->rows->base : nullptr;
-    e = rows_alloc(*s, b.padded_n, b.total_axons);
+    e = rows_alloc(*s, b.padded_n, b.total_axons, true, stream);
     if (e != cudaSuccess) return e;
     realloc = realloc || (before != nullptr && before != s->rows->base);
   }
@@ -259,8 +259,8 @@ extern "C" int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_
   rows_touched(*s);
   if (rows) {
     bool realloc = false;
-    e = ensure_counts(*s, ticks ? ticks : 1, &realloc);
-    if (e == cudaSuccess) e = rows_alloc(*s, padded_n, total_axons);
+    e = ensure_counts(*s, ticks ? ticks : 1, &realloc, st);
+    if (e == cudaSuccess) e = rows_alloc(*s, padded_n, total_axons, true, st);
     if (e != cudaSuccess) return (int32_t)e;
     if (realloc && s->graph_cache) {
       GraphCache* old = static_cast<GraphCache*>(s->graph_cache);

@@ -70,6 +70,7 @@ struct RowCache {
   uint32_t* wcnt = nullptr; // [2][kMaxUpdateWarps] spikers each warp of the update pass listed (gs_n, gd_n)
   int2* lsum = nullptr;     // [N] x: wrapping sum of the row's lit-sum weights, y: row positions before them
   uint32_t* xlit = nullptr; // [A/32+1] axons taken as fully lit when the row layout was made
+  uint8_t* posmap = nullptr;  // [N][128] row position of each columnar slot (learned engine only; own allocation)
 };
 
 // Per-shard scratch owned by the engine, next to the reference-visible
@@ -104,9 +105,13 @@ constexpr uint32_t kFixCap = 1u << 22;  // deferred GSOP slots per tick before t
 constexpr uint32_t kMaxUpdateWarps = 32u * 1024u;  // warps of the update pass (32 per SM)
 
 // Row engine (row_engine.cuh, compiled in day_phase.cu).  A (re)allocation
-// drops the batch engine's captured graphs, which hold the old addresses.
-cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix = true);
+// drops the batch engine's captured graphs, which hold the old addresses; the
+// new buffers are zeroed on `stream` (the legacy stream: zeroed before return).
+cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix, cudaStream_t stream);
 void rows_free(ShardScratch& s);
+// Allocates the row copy's position map (row position of every columnar slot),
+// written by every later row copy of the shard.
+cudaError_t rows_posmap(ShardScratch& s, cudaStream_t stream);
 // row_sum: also compute the targets checksum (ShardCtl::row_sum) the learned engine checks its index against.
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
                               bool row_sum = false, bool permute = true);

@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
                                                        const uint8_t* __restrict__ inv_seg,
                                                        const uint2* __restrict__ mask2,
                                                        const int16_t* __restrict__ rw,
+                                                       const uint8_t* __restrict__ posmap,
                                                        const uint8_t* __restrict__ flags,
                                                        const BurstHeads8* __restrict__ heads, uint32_t A,
                                                        int32_t* __restrict__ acc, ShardCtl* __restrict__ sc) {
@@ -323,7 +324,9 @@ __global__ void __launch_bounds__(256) k_learn_scatter(LearnDev L, uint32_t T, c
       const uint32_t n = slot / kRowStride;
       const uint32_t evw = __ldg(L.evbits + (n >> 5));
       const uint32_t fl = flags[n];
-      const int32_t wv = rw[slot];
+      // the index holds columnar slots; the row copy keeps the slots whose weights
+      // may still move first, so the weight sits at the row position the map gives
+      const int32_t wv = rw[(size_t)n * kRowStride + __ldg(posmap + slot)];
       if (!((evw >> (n & 31u)) & 1u)) continue;
       const uint32_t prop = s_prop[fl >> 4];
       bool hit = true;
@@ -752,6 +755,12 @@ __global__ void __launch_bounds__(128) k_mlp_predict(const __nv_bfloat16* __rest
 namespace axc {
 namespace {
 
+// After chunks on the plain graph the features history is stale: the next
+// learned tick plans without the previous tick's features (no prediction, dense).
+__global__ void k_learn_resume(LearnCtl* c) { c->feat_done = 0; }
+
+constexpr uint32_t kGateMin = 4, kGateMax = 64;   // chunks on the plain graph after a dense-only probe
+
 __global__ void k_learn_set_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopamine) {
   ctl->tick_base = tick_base;
   ctl->dopamine = dopamine;
@@ -793,6 +802,12 @@ struct Learned {
   uint32_t adam_step = 0;
   int32_t policy = -1;
   uint32_t collect = 0;
+  // gate: while the predictor keeps choosing the dense form, chunks run on a
+  // plain graph (no features, no plan); gate_len doubles after every probe that
+  // chose dense throughout (up to kGateMax chunks), back to kGateMin after one
+  // that chose sparse
+  uint32_t gate_left = 0, gate_len = 0;
+  uint64_t gated_ticks = 0;
   const void* rows_base = nullptr;   // the row cache the graphs were captured with
   std::map<std::tuple<uint32_t, uint32_t>, cudaGraphExec_t> graphs;
   cudaStream_t capture = nullptr;
@@ -841,7 +856,7 @@ static cudaError_t learned_index(Learned& L, cudaStream_t st) {
   cudaError_t e;
   ShardScratch* s = scratch_for(&L.v, L.N, L.A, &e);
   if (!s) return e;
-  e = rows_alloc(*s, L.N, L.A);
+  e = rows_alloc(*s, L.N, L.A, true, st);
   if (e != cudaSuccess) return e;
   rows_touched(*s);   // slot-order rows replace the per-tick entry point's
   e = launch_rows_begin(L.v, *s, L.N, L.A, st, true, false);
@@ -894,14 +909,19 @@ static void learned_update_forms(Learned& L, ShardScratch& s, uint32_t k, cudaSt
   const int sms = sm_count();
   const LearnDev D = L.dev();
   const uint32_t fix_cap = kFixCap;
-  launch_rows_update<false>(L.v, s, N, A, k, fix_cap, L.ctl, st);
-  k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw,
+  // dense: the plain engine's passes on the movable-first rows, GSOP inside them
+  // (the 8-lane pass, or the lit-sum form when its lit set held)
+  launch_rows_update<true>(L.v, s, N, A, k, fix_cap, L.ctl, st);
+  k_rows_update_lsum<false><<<kLsumBlocks * sms, 256, 0, st>>>(L.v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend,
+                                                               r.fix, s.ctl, k, fix_cap, r.lit, r.lfz, r.lsum,
+                                                               ColWT{}, L.ctl);
+  // sparse: the axon-driven gather, GLIF, and GSOP of the spikers it listed
+  k_learn_scatter<<<8 * sms, 256, ((size_t)L.T + 1) * 4, st>>>(D, L.T, L.inv, L.inv_seg, r.mask2, r.rw, r.posmap,
                                                                 L.v.soma_flags, L.v.axon_heads, A, L.acc, s.ctl);
   // 4 blocks of 256 per SM: the 32 warps per SM whose slices the GSOP passes read
   k_learn_update<<<4 * sms, 256, 0, st>>>(L.v, D, A, r.cnt, r.eval, s.pend, L.acc, r.lfz, r.gs_n, r.gd_n, r.wcnt,
                                           s.ctl, k);
-  // GSOP of the spikers listed by whichever form ran
-  launch_rows_gsop(L.v, s, A, k, fix_cap, st);
+  launch_rows_gsop(L.v, s, A, k, fix_cap, st, L.ctl);
 }
 
 // One tick: schedule, prologue, both update forms (the one not picked returns
@@ -920,7 +940,7 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool la
     k_rows_prologue<true><<<(G + 255) / 256, 256, 0, st>>>(L.v.axon_heads, A, L.v_seg, bits_k, L.voff,
                                                            bits_k ? L.nv : 0u, s.incoming, nullptr, k, r.mask2,
                                                            r.mult, L.v.soma_flags, L.v.timers, N, r.eval, s.ctl,
-                                                           raise, r.lit, D, k > 0 ? s.pend : nullptr);
+                                                           raise, r.lit, D, k > 0 ? s.pend : nullptr, r.xlit);
   learned_update_forms(L, s, k, st);
   k_rows_fixup<<<2 * sms, 256, 0, st>>>(L.v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, k,
                                         nullptr, nullptr, 0, ColWT{});
@@ -1067,6 +1087,8 @@ int32_t axc_learned_set_policy(void* handle, int32_t policy, float ratio, float 
   hc.margin = margin;
   hc.slack = slack;
   L->policy = policy;
+  L->gate_left = 0;
+  L->gate_len = 0;
   return (int32_t)cudaMemcpy(L->ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice);
 }
 
@@ -1097,7 +1119,8 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   cudaError_t e;
   ShardScratch* s = scratch_for(&L->v, L->N, L->A, &e);
   if (!s) return (int32_t)e;
-  e = rows_alloc(*s, L->N, L->A);
+  e = rows_alloc(*s, L->N, L->A, true, st);
+  if (e == cudaSuccess) e = rows_posmap(*s, st);
   if (e != cudaSuccess) return (int32_t)e;
   rows_touched(*s);
   if (L->rows_base != s->rows->base) {
@@ -1114,28 +1137,52 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     L->drop_graphs();
   }
   const bool features_on = L->policy < 0 || L->collect;
-  const auto key = std::make_tuple(tpg, features_on ? 1u : 0u);
-  cudaGraphExec_t exec = nullptr;
-  auto it = L->graphs.find(key);
-  if (it != L->graphs.end()) {
-    exec = it->second;
-  } else {
-    e = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return (int32_t)e;
-    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true, false);
-    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++)
-      le = learned_tick(*L, *s, k, k + 1 == tpg, features_on, L->capture);
+  // graph kinds: 0/1 learned (features off/on), 2 plain (the gate)
+  auto graph_of = [&](uint32_t kind, cudaGraphExec_t* out) -> cudaError_t {
+    const auto key = std::make_tuple(tpg, kind);
+    auto it = L->graphs.find(key);
+    if (it != L->graphs.end()) {
+      *out = it->second;
+      return cudaSuccess;
+    }
+    cudaError_t ce = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) return ce;
+    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true, true);
+    for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) {
+      if (kind == 2) {   // the plain engine's tick on the staged bitmask rows
+        TickArgs a{};
+        a.padded_n = L->N;
+        a.total_axons = L->A;
+        a.v_seg = L->v_seg;
+        a.input_bitmask = L->nv ? L->stage + (size_t)k * L->words : nullptr;
+        a.virtual_offset = L->voff;
+        a.num_virtual = a.input_bitmask ? L->nv : 0u;
+        a.batch = true;
+        a.k = k;
+        a.rows = true;
+        a.defer_push = k + 1 < tpg;
+        a.fix_cap = kFixCap;
+        le = launch_tick(L->v, *s, a, L->capture);
+      } else {
+        le = learned_tick(*L, *s, k, k + 1 == tpg, kind == 1, L->capture);
+      }
+    }
     if (le == cudaSuccess) le = launch_rows_end(L->v, *s, L->N, L->capture);
     cudaGraph_t g = nullptr;
-    e = cudaStreamEndCapture(L->capture, &g);
-    if (le != cudaSuccess) e = le;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+    ce = cudaStreamEndCapture(L->capture, &g);
+    if (le != cudaSuccess) ce = le;
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(out, g, 0);
     if (g) cudaGraphDestroy(g);
-    if (e != cudaSuccess) return (int32_t)e;
-    L->graphs[key] = exec;
-  }
+    if (ce == cudaSuccess) L->graphs[key] = *out;
+    return ce;
+  };
+  const bool gate_on = L->policy < 0 && !L->collect;
   for (uint32_t c = 0; c < ticks / tpg && e == cudaSuccess; c++) {
     const uint32_t t0 = tick0 + c * tpg;
+    const bool gated = gate_on && L->gate_left > 0;
+    cudaGraphExec_t exec = nullptr;
+    e = graph_of(gated ? 2u : (features_on ? 1u : 0u), &exec);
+    if (e != cudaSuccess) break;
     if (L->bits) {
       const uint32_t have = std::min(tpg + 1, L->bits_ticks - t0);
       e = cudaMemcpyAsync(L->stage, L->bits + (size_t)t0 * L->words, (size_t)have * L->words * 4,
@@ -1146,7 +1193,29 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     }
     k_learn_set_ctl<<<1, 1, 0, st>>>(s->ctl, L->tick_base + t0, (int32_t)L->dopamine);
     e = launch_reset_burst(L->v, L->N, st);
+    unsigned long long picked0 = 0, picked1 = 0;
+    const size_t picked_at = offsetof(LearnCtl, stat) + kStSparsePicked * sizeof(unsigned long long);
+    if (e == cudaSuccess && gate_on && !gated)
+      e = cudaMemcpyAsync(&picked0, reinterpret_cast<char*>(L->ctl) + picked_at, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+    if (e != cudaSuccess) break;
+    if (gated) {
+      L->gate_left--;
+      L->gated_ticks += tpg;
+      if (L->gate_left == 0) k_learn_resume<<<1, 1, 0, st>>>(L->ctl);   // the features history is stale
+      continue;
+    }
+    if (!gate_on) continue;
+    // a probe chunk: did the predictor choose the sparse form on any tick?
+    e = cudaMemcpyAsync(&picked1, reinterpret_cast<char*>(L->ctl) + picked_at, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) break;
+    if (picked1 == picked0) {
+      L->gate_len = L->gate_len ? std::min(2 * L->gate_len, kGateMax) : kGateMin;
+      L->gate_left = L->gate_len;
+    } else {
+      L->gate_len = 0;
+    }
   }
   return (int32_t)e;
 }
@@ -1159,6 +1228,7 @@ int32_t axc_learned_stats(void* handle, uint64_t* out16) {
   if (e == cudaSuccess) e = cudaMemcpy(&hc, L->ctl, sizeof(hc), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return (int32_t)e;
   for (int q = 0; q < 12; q++) out16[q] = hc.stat[q];
+  out16[9] = L->gated_ticks;
   out16[12] = hc.samples;
   out16[13] = hc.ticks_seen;
   out16[14] = hc.T;
@@ -1172,6 +1242,8 @@ int32_t axc_learned_reset_stats(void* handle) {
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess)
     e = cudaMemset(reinterpret_cast<char*>(L->ctl) + offsetof(LearnCtl, stat), 0, sizeof(LearnCtl::stat));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);   // cleared before a run on any stream
+  L->gated_ticks = 0;
   return (int32_t)e;
 }
 
@@ -1188,6 +1260,7 @@ int32_t axc_learned_params(void* handle, float* host_out, const float* host_in) 
       k_mlp_to_bf16<<<(kParams + 255) / 256, 256>>>(L->master, L->wb);
       e = cudaGetLastError();
     }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);   // in place before a run on any stream
     L->adam_step = 0;
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();

@@ -701,7 +701,7 @@ int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, voi
     const AxcPopBrainDesc& d = brains[b];
     ShardScratch* s = scratch_for(&d.vram, d.padded_n, d.total_axons, &e);
     if (!s) break;
-    e = rows_alloc(*s, d.padded_n, d.total_axons, false);
+    e = rows_alloc(*s, d.padded_n, d.total_axons, false, nullptr);
     if (e != cudaSuccess) break;
     rows_touched(*s);
     P->scr.push_back(s);
@@ -756,6 +756,7 @@ int32_t axc_population_create(const AxcPopBrainDesc* brains, uint32_t count, voi
   if (e == cudaSuccess) e = cudaMalloc(&P->d_fix, (size_t)kFixCap * sizeof(uint2));
   if (e == cudaSuccess) e = cudaMalloc(&P->d_ctl, sizeof(PopCtl));
   if (e == cudaSuccess) e = cudaMemset(P->d_ctl, 0, sizeof(PopCtl));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);   // zeroed before a run on any stream
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&P->capture, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     pop_free(P);

@@ -310,7 +310,7 @@ __device__ __forceinline__ RowBuilt build_row(uint32_t (*s_t)[33], const int16_t
                                               uint16_t* __restrict__ cnt, uint4* __restrict__ amask,
                                               uint4* __restrict__ omask, uint8_t* __restrict__ lfz,
                                               const uint32_t* __restrict__ xlit = nullptr, bool exact_var = false,
-                                              int2* __restrict__ lsum = nullptr) {
+                                              int2* __restrict__ lsum = nullptr, uint8_t* __restrict__ posmap = nullptr) {
   const uint32_t lane = threadIdx.x & 31;
   const bool lsum_on = permute && xlit != nullptr && exact_var;
   bool bad = false;
@@ -379,6 +379,7 @@ __device__ __forceinline__ RowBuilt build_row(uint32_t (*s_t)[33], const int16_t
     if (q < c) {
       rt[(size_t)n * kRowStride + pos] = s_t[q][j];
       rw[(size_t)n * kRowStride + pos] = s_w[q][j];
+      if (posmap) posmap[(size_t)n * kRowStride + q] = (uint8_t)pos;
     }
     // the movable slots by row position: the first lf positions, or mv itself
     const uint32_t lo = 32u * ch;
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
                                                     uint4* __restrict__ omask, uint8_t* __restrict__ lfz,
                                                     ShardCtl* __restrict__ ctl, uint32_t A, uint32_t want_sum,
                                                     uint32_t permute, const uint32_t* __restrict__ xlit,
-                                                    int2* __restrict__ lsum) {
+                                                    int2* __restrict__ lsum, uint8_t* __restrict__ posmap) {
   __shared__ uint32_t s_t[AXC_MAX_DENDRITES][33];
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_cnt[32];
@@ -489,7 +490,7 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
     const uint32_t c = s_cnt[j];
     const VariantParameters& vp = VARIANT_LUT[flags[n] >> 4];
     const RowBuilt rb = build_row(s_t, s_w, j, n, c, frozen_from(vp), A, want_sum != 0u, permute != 0u, rt, rw, cnt,
-                                  amask, omask, lfz, xlit, vp.signal_propagation_length == s_pmax, lsum);
+                                  amask, omask, lfz, xlit, vp.signal_propagation_length == s_pmax, lsum, posmap);
     if (lane == 0 && c) {
       wc = max(wc, c);
       ws = max(ws, rb.smx);
@@ -606,10 +607,12 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
                                                        uint32_t N, uint32_t* __restrict__ eval,
                                                        ShardCtl* __restrict__ ctl, uint32_t raise_err,
                                                        uint32_t* __restrict__ lit_bits, LearnDev L,
-                                                       uint32_t* __restrict__ pend_apply) {
+                                                       uint32_t* __restrict__ pend_apply,
+                                                       const uint32_t* __restrict__ xlit) {
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[8];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t xw = (xlit && i < A) ? __ldg(xlit + (i >> 5)) : 0u;   // axons the row layout took as fully lit
   // every load first, with no barrier before them: heads, owners, pending
   // pushes, input bit; the batch constants are read by every thread (the LUT's
   // largest length and the largest segment, both set by the row copy)
@@ -672,7 +675,10 @@ __global__ void __launch_bounds__(256) k_rows_prologue(BurstHeads8* __restrict__
   if (LEARN) learn_axons(L, i, A, fan, inflight);
   if (lit_bits) {
     const uint32_t lb = __ballot_sync(kFull, lit);
-    if ((threadIdx.x & 31) == 0 && i < A) lit_bits[i >> 5] = lb;
+    if ((threadIdx.x & 31) == 0 && i < A) {
+      lit_bits[i >> 5] = lb;
+      if (xw & ~lb) atomicOr(&ctl->dense[k & 1], 1u);   // the lit-sum form cannot run this tick
+    }
   }
   bool ev = false;
   if (i < N) {
@@ -1250,7 +1256,9 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
                                                           uint32_t k, uint32_t fix_cap,
                                                           const uint32_t* __restrict__ lit_bits,
                                                           const uint8_t* __restrict__ lfz,
-                                                          const int2* __restrict__ lsum, ColWT wt) {
+                                                          const int2* __restrict__ lsum, ColWT wt,
+                                                          const LearnCtl* __restrict__ lc) {
+  if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
   if (!lsum_tick(ctl, k)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ctr[6] += 1;   // ticks on the lit-sum form
   __shared__ VariantParameters lut[16];
@@ -1373,7 +1381,9 @@ __global__ void __launch_bounds__(256) k_rows_gsop(ShardVramPtrs P, uint32_t A, 
                                                    const uint32_t* __restrict__ wcnt, uint32_t nwu,
                                                    uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl, uint32_t k,
                                                    uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
-  (void)lc;   // the learned engine lists its sparse ticks' spikers here too
+  // the learned engine lists the spikers of its sparse ticks here; on its dense
+  // ticks the update pass applied GSOP itself
+  if (lc && !(lc->mode == 1u && !lc->overflow)) return;
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
@@ -1487,7 +1497,7 @@ __global__ void __launch_bounds__(256) k_rows_gsop_rows(ShardVramPtrs P, uint32_
                                                         const uint32_t* __restrict__ wcnt, uint32_t nwu,
                                                         uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
                                                         uint32_t k, uint32_t fix_cap, const LearnCtl* __restrict__ lc) {
-  (void)lc;   // the learned engine lists its sparse ticks' spikers here too
+  if (lc && !(lc->mode == 1u && !lc->overflow)) return;   // as k_rows_gsop
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
@@ -1832,7 +1842,7 @@ uint32_t set_first_wait_limit(uint32_t tries) {
   return prev;
 }
 
-cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
+cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix, cudaStream_t stream) {
   if (s.rows && s.rows->N >= N && s.rows->A >= A && (s.rows->fix || !with_fix)) return cudaSuccess;
   graph_cache_drop(&s);   // captured graphs hold the old buffers' addresses
   rows_touched(s);
@@ -1858,7 +1868,12 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
   if (e != cudaSuccess) return e;
-  e = cudaMemset(base, 0, off);
+  // zeroed in the order of the caller's stream: a blocking memset would go on
+  // the legacy stream, which a non-blocking stream does not wait for (work
+  // queued there before it, another shard's graph say, would delay the zeroing
+  // into this shard's first batch)
+  e = cudaMemsetAsync(base, 0, off, stream);
+  if (e == cudaSuccess && stream == nullptr) e = cudaStreamSynchronize(nullptr);
   if (e != cudaSuccess) { cudaFree(base); return e; }
   RowCache* r = new RowCache();
   char* b = static_cast<char*>(base);
@@ -1885,8 +1900,19 @@ cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix) {
   return cudaSuccess;
 }
 
+cudaError_t rows_posmap(ShardScratch& s, cudaStream_t stream) {
+  if (!s.rows) return cudaErrorInvalidValue;
+  if (s.rows->posmap) return cudaSuccess;
+  const size_t bytes = (size_t)s.rows->N * kRowStride;
+  cudaError_t e = cudaMalloc(&s.rows->posmap, bytes ? bytes : 1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.rows->posmap, 0, bytes, stream);
+  if (e == cudaSuccess) graph_cache_drop(&s);   // graphs captured without the map do not write it
+  return e;
+}
+
 void rows_free(ShardScratch& s) {
   if (!s.rows) return;
+  if (s.rows->posmap) cudaFree(s.rows->posmap);
   cudaFree(s.rows->base);
   delete s.rows;
   s.rows = nullptr;
@@ -1910,7 +1936,8 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
     k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, v.soma_flags, N, r.rt,
                                                     r.rw, r.cnt, r.amask, r.omask, r.lfz, s.ctl, A,
                                                     row_sum ? 1u : 0u, permute ? 1u : 0u,
-                                                    permute ? r.xlit : nullptr, permute ? r.lsum : nullptr);
+                                                    permute ? r.xlit : nullptr, permute ? r.lsum : nullptr,
+                                                    r.posmap);
   }
   return cudaGetLastError();
 }
@@ -1978,21 +2005,19 @@ static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t
 // The GSOP passes over the spikers the tick's update pass listed (32 warps per
 // SM, each with its slice of the evaluated list; a GSOP warp per slice).
 static void launch_rows_gsop(const ShardVramPtrs& v, ShardScratch& s, uint32_t A, uint32_t k, uint32_t fix_cap,
-                             cudaStream_t stream) {
+                             cudaStream_t stream, const LearnCtl* lc = nullptr) {
   RowCache& r = *s.rows;
   const uint32_t nwu = (uint32_t)sm_count() * 32u;
   if (rows_lit(A)) {
     k_rows_gsop<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
-                                                   nwu, r.fix, s.ctl, k, fix_cap, nullptr);
+                                                   nwu, r.fix, s.ctl, k, fix_cap, lc);
     k_rows_gsop_rows<true><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
-                                                        r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap,
-                                                        nullptr);
+                                                        r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap, lc);
   } else {
     k_rows_gsop<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.amask, r.gs_n, r.wcnt,
-                                                    nwu, r.fix, s.ctl, k, fix_cap, nullptr);
+                                                    nwu, r.fix, s.ctl, k, fix_cap, lc);
     k_rows_gsop_rows<false><<<nwu / 8, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.lit, r.gd_n,
-                                                         r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap,
-                                                         nullptr);
+                                                         r.wcnt + kMaxUpdateWarps, nwu, r.fix, s.ctl, k, fix_cap, lc);
   }
 }
 
@@ -2033,10 +2058,10 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   launch_rows_update<true>(v, s, N, A, a.k, fix_cap, nullptr, stream, wt);
   if (per_tick)
     k_rows_update_lsum<true><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                          s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt);
+                                                          s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt, nullptr);
   else
     k_rows_update_lsum<false><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                           s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt);
+                                                           s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt, nullptr);
   if (ev) cudaEventRecord(ev[3], stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,

@@ -37,7 +37,10 @@ cudaError_t scratch_alloc(ShardScratch* s, uint32_t N, uint32_t A) {
   void* base = nullptr;
   cudaError_t e = cudaMalloc(&base, off);
   if (e != cudaSuccess) return e;
+  // zeroed before return: the scratch may be created by a call on a
+  // non-blocking stream, which would not wait for a memset on the legacy stream
   e = cudaMemset(base, 0, off);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
   if (e != cudaSuccess) { cudaFree(base); return e; }
   char* b = static_cast<char*>(base);
   s->base = base;
@@ -272,7 +275,7 @@ int32_t cu_step_day_phase(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
   // copy the columnar kernels run the tick.
   bool rows = g_tick_mode.load() == 1 && padded_n > 0 && total_axons > 0;
   if (rows && !(s->rows && s->rows->N >= padded_n && s->rows->A >= total_axons)) {
-    if (rows_alloc(*s, padded_n, total_axons) != cudaSuccess) {
+    if (rows_alloc(*s, padded_n, total_axons, true, st) != cudaSuccess) {
       cudaGetLastError();   // the failed allocation's error is not this tick's
       rows = false;
     }
@@ -441,6 +444,7 @@ int32_t axc_shard_error_flags(const ShardVramPtrs* vram, uint32_t clear, uint32_
   if (e != cudaSuccess) return (int32_t)e;
   e = cudaMemcpy(out_flags, &s->ctl->err, 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && clear) e = cudaMemset(&s->ctl->err, 0, 4);
+  if (e == cudaSuccess && clear) e = cudaDeviceSynchronize();   // cleared before any later stream's work
   return (int32_t)e;
 }
 
@@ -452,6 +456,7 @@ int32_t axc_shard_counters(const ShardVramPtrs* vram, uint32_t reset, uint64_t o
   if (e != cudaSuccess) return (int32_t)e;
   e = cudaMemcpy(out, s->ctl->ctr, 8 * sizeof(uint64_t), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && reset) e = cudaMemset(s->ctl->ctr, 0, 8 * sizeof(uint64_t));
+  if (e == cudaSuccess && reset) e = cudaDeviceSynchronize();
   return (int32_t)e;
 }
 

@@ -20,7 +20,7 @@ FEATURES, HIDDEN = 64, 128
 TILE = 1024
 
 STAT_NAMES = ("ticks", "sparse_ticks", "overflow_reruns", "schedule_mismatches", "abs_err_synapses",
-              "actual_synapses", "judged_ticks", "planned_sparse", "stale_ticks", "r9", "r10", "r11",
+              "actual_synapses", "judged_ticks", "planned_sparse", "stale_ticks", "gated_ticks", "r10", "r11",
               "samples", "history", "tiles", "index_capacity")
 
 

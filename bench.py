@@ -642,7 +642,8 @@ def run_learned(args) -> None:
     training; [trace, total-200): the predictor's schedule (timed);
     [total-200, total): the predictor running but the schedule forced dense
     (the learned engine's cost over the plain path when it never goes
-    sparse, in the steady state).  The plain copy of the brain runs the same
+    sparse, in the steady state: with the gate, mostly chunks on the plain
+    graph and a probe now and then).  The plain copy of the brain runs the same
     ticks through axc_step_day_phase_batch; final states are compared."""
     import hashlib
     import torch
@@ -751,6 +752,7 @@ def run_learned(args) -> None:
         "bitexact_vs_plain": same,
         "predictor": {
             "sparse_ticks": st["sparse_ticks"], "planned_sparse": st["planned_sparse"],
+            "gated_ticks": st["gated_ticks"],
             "overflow_reruns": st["overflow_reruns"],
             "misprediction_rate": st["overflow_reruns"] / max(st["planned_sparse"], 1),
             "schedule_mismatch_rate": st["schedule_mismatches"] / max(st["judged_ticks"], 1),

@@ -517,8 +517,14 @@ int32_t axc_learned_samples(void* handle, uint32_t first, uint32_t count, float*
 /* [0] ticks, [1] sparse ticks, [2] overflow re-runs, [3] schedule mismatches
  * against exact counts, [4] sum |predicted - actual| active synapses over
  * tiles, [5] sum actual, [6] judged ticks, [7] planned sparse, [8] stale-index
- * ticks, [12] recorded pairs, [13] feature history length, [14] tiles,
- * [15] index capacity. */
+ * ticks, [9] ticks run with the predictor gated off, [12] recorded pairs,
+ * [13] feature history length, [14] tiles, [15] index capacity.
+ * Gate (policy -1, not collecting): a chunk of ticks_per_graph ticks in which
+ * the predictor chose the dense form on every tick is followed by 4 chunks on
+ * the plain engine's graph (no features, no plan), then a probe chunk with the
+ * predictor; each dense-only probe doubles the gate (up to 64 chunks), a probe
+ * that chose the sparse form ends it.  Dense ticks of both graphs run the
+ * plain engine's passes, so the state is the same either way. */
 int32_t axc_learned_stats(void* handle, uint64_t out[16]);
 int32_t axc_learned_reset_stats(void* handle);
 void axc_learned_destroy(void* handle);

@@ -51,8 +51,9 @@ def frozen_brain(seed=3, mixed_lengths=False):
 
 
 def silencing_lut(lut):
+    """Excitatory neurons never reach threshold: their axons leave the fully-lit set within ~28 ticks."""
     quiet = lut.copy()
-    quiet[0]["threshold"] = 60000
+    quiet[0]["threshold"] = 1 << 30
     return quiet
 
 
