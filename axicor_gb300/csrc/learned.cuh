@@ -42,6 +42,7 @@ constexpr uint32_t kHistCh = 4;            // spikes, active synapses, heads in 
 constexpr uint32_t kHistLen = 8;
 constexpr uint32_t kHistF = kHistCh * kHistLen + 1;   // + the tile's next-tick evaluated count
 constexpr uint32_t kGradPer = 16;          // samples per block of the gradient kernel
+constexpr uint32_t kResidF = 8;            // the tile's active-synapse fraction of the tick just run
 
 // LearnCtl.stat[]
 enum : int {
@@ -84,7 +85,10 @@ __device__ __forceinline__ float mlp_unit(const __nv_bfloat16* __restrict__ wb, 
 }
 
 // Output of the MLP for the input in xs, computed by a 128-thread block
-// (thread u = hidden unit u); a fixed reduction order, so deterministic.
+// (thread u = hidden unit u); a fixed reduction order, so deterministic.  The
+// network predicts a residual: its output is added to input kResidF (the
+// tile's active-synapse fraction of the tick just run), so zero weights give
+// the last-tick rule and training learns the change from tick to tick.
 __device__ __forceinline__ float mlp_block_forward(const __nv_bfloat16* __restrict__ wb, const float* xs, float* red,
                                                    float* a_out, float* hb_out) {
   const uint32_t u = threadIdx.x;
@@ -95,8 +99,9 @@ __device__ __forceinline__ float mlp_block_forward(const __nv_bfloat16* __restri
   __syncthreads();
   if ((u & 31) == 0) red[u >> 5] = part;
   __syncthreads();
-  const float y = __fadd_rn(__fadd_rn(__fadd_rn(red[0], red[1]), __fadd_rn(red[2], red[3])),
-                            __bfloat162float(wb[kOffB2]));
+  const float y = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(red[0], red[1]), __fadd_rn(red[2], red[3])),
+                                      __bfloat162float(wb[kOffB2])),
+                            xs[kResidF]);
   if (a_out) *a_out = a;
   if (hb_out) *hb_out = hb;
   return y;
@@ -1040,13 +1045,13 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
   hc.margin = 0.25f;
   hc.slack = 64;
   hc.T = T;
-  // seeded uniform init (fan-in scaled), biases 0
+  // seeded uniform init of W1 (fan-in scaled); biases and w2 zero, so the
+  // untrained network predicts the last-tick rule
   std::vector<float> w(kParams, 0.f);
   uint64_t sd = 0xA11CE5EEDull;
   for (uint32_t p = 0; p < kParams; p++) {
     const float u = (float)(smix(sd) >> 40) * (1.f / 16777216.f) * 2.f - 1.f;
-    if (p < kOffB1) w[p] = u * 0.30618622f;              // sqrt(6 / 64)
-    else if (p >= kOffW2 && p < kOffB2) w[p] = u * 0.21650635f;   // sqrt(6 / 128)
+    if (p < kOffB1) w[p] = u * 0.30618622f;   // sqrt(6 / 64)
   }
   e = cudaMemcpy(L->ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(L->master, w.data(), (size_t)kParams * 4, cudaMemcpyHostToDevice);

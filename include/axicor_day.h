@@ -471,7 +471,9 @@ uint32_t axc_population_fix_capacity(uint32_t cap);
 
 /* ---- Learned-schedule engine ------------------------------------------- */
 /* One brain stepped by the row engine, with a per-tile activity predictor (an
- * MLP 64 -> 128 -> 1, BF16 weights, FP32 accumulation; tiles of 1024 axons)
+ * MLP 64 -> 128 -> 1, BF16 weights, FP32 accumulation; tiles of 1024 axons;
+ * the output is a residual added to input 8, the tile's active-synapse
+ * fraction of the tick just run, so zero weights are the last-tick rule)
  * choosing before every tick between the dense row pass and a sparse,
  * axon-driven gather through an inverted index, and sizing the per-tile
  * compaction buffers of the sparse form.  A tile that outgrows its buffer

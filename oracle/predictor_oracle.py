@@ -9,7 +9,8 @@ value for value:
 - hidden unit u: a = b1[u], then a = fma(W1[u][k], x[k], a) for k = 0..63;
   hb = bf16(relu(a)); part = w2[u] * hb (exact in FP32);
 - output: a butterfly sum over each warp of 32 units (xor 16, 8, 4, 2, 1),
-  then (w0 + w1) + (w2 + w3), then + b2;
+  then (w0 + w1) + (w2 + w3), then + b2, then + x[RESID] (the network
+  predicts the change from the last tick's active-synapse fraction);
 - loss = mean (y - t)^2 accumulated as fma(d * d, 1/B, loss); dy = (2 d)(1/B);
   per block of 16 samples, in sample order: gw2 = fma(dy, hb, gw2),
   gb2 += dy, dh = dy * w2 if a > 0 else 0, gb1 += dh, g1[k] = fma(dh, x[k], g1[k]);
@@ -29,6 +30,7 @@ OFF_W2 = OFF_B1 + HIDDEN
 OFF_B2 = OFF_W2 + HIDDEN
 PARAMS = OFF_B2 + 1
 GRAD_PER = 16
+RESID = 8
 f32 = np.float32
 
 
@@ -64,6 +66,7 @@ def forward(params: np.ndarray, x: np.ndarray):
     r = v[:, :, 0]
     y = ((r[:, 0] + r[:, 1]).astype(np.float32) + (r[:, 2] + r[:, 3]).astype(np.float32)).astype(np.float32)
     y = (y + f32(b2)).astype(np.float32)
+    y = (y + xb[:, RESID]).astype(np.float32)
     return y, a, hb
 
 
@@ -107,7 +110,7 @@ def loss_float64(params: np.ndarray, x: np.ndarray, t: np.ndarray) -> float:
     p = np.asarray(params, np.float64)
     W1 = p[:OFF_B1].reshape(HIDDEN, FEATURES)
     a = np.asarray(x, np.float64) @ W1.T + p[OFF_B1:OFF_W2]
-    y = np.maximum(a, 0) @ p[OFF_W2:OFF_B2] + p[OFF_B2]
+    y = np.maximum(a, 0) @ p[OFF_W2:OFF_B2] + p[OFF_B2] + np.asarray(x, np.float64)[:, RESID]
     return float(np.mean((y - np.asarray(t, np.float64)) ** 2))
 
 
@@ -118,7 +121,7 @@ def grad_float64(params: np.ndarray, x: np.ndarray, t: np.ndarray) -> np.ndarray
     xd = np.asarray(x, np.float64)
     a = xd @ W1.T + p[OFF_B1:OFF_W2]
     h = np.maximum(a, 0)
-    y = h @ p[OFF_W2:OFF_B2] + p[OFF_B2]
+    y = h @ p[OFF_W2:OFF_B2] + p[OFF_B2] + xd[:, RESID]
     dy = 2.0 * (y - np.asarray(t, np.float64)) / x.shape[0]
     dh = (dy[:, None] * p[OFF_W2:OFF_B2][None, :]) * (a > 0)
     g = np.zeros(PARAMS)

@@ -3,9 +3,9 @@
 The learned engine sizes each tile's compaction buffer for a sparse tick from
 the predicted active synapses of the next tick; an under-prediction overflows
 the buffer and the tick re-runs dense (exact, but slower).  The baseline is
-the last-tick rule, "next tick's activity = this tick's", written as weights
-of the same MLP (one hidden unit passes feature 8, the tile's active-synapse
-fraction of the tick just run, through the ReLU unchanged), so both run
+the last-tick rule, "next tick's activity = this tick's": the network
+predicts a residual on feature 8 (the tile's active-synapse fraction of the
+tick just run), so all-zero weights are exactly that rule, and both run
 through the same kernels on the same ticks of a quiet brain (homeostasis on,
 input rate following a 100-tick sinusoid).  The trained network must predict
 the held-out pairs with a lower error and mispredict fewer planned sparse
@@ -22,15 +22,11 @@ from test_learned_gpu import LBrain
 
 pytestmark = pytest.mark.gpu
 
-FEAT, HID = 64, 128
 LAST_TICK_FEATURE = 8   # channel 1 (active-synapse fraction), lag 0
 
 
 def last_tick_params():
-    p = np.zeros(L.param_count(), np.float32)
-    p[0 * FEAT + LAST_TICK_FEATURE] = 1.0       # W1[0][8]
-    p[HID * FEAT + HID + 0] = 1.0               # w2[0]
-    return p
+    return np.zeros(L.param_count(), np.float32)   # output = feature 8 + 0
 
 
 def test_trained_predictor_beats_last_tick_rule(gpu):
