@@ -110,11 +110,12 @@ constexpr uint32_t kMaxUpdateWarps = 32u * 1024u;  // warps of the update pass (
 cudaError_t rows_alloc(ShardScratch& s, uint32_t N, uint32_t A, bool with_fix, cudaStream_t stream);
 void rows_free(ShardScratch& s);
 // Allocates the row copy's position map (row position of every columnar slot),
-// written by every later row copy of the shard.
+// written by every later row copy of the shard that asks for it.
 cudaError_t rows_posmap(ShardScratch& s, cudaStream_t stream);
-// row_sum: also compute the targets checksum (ShardCtl::row_sum) the learned engine checks its index against.
+// row_sum: also compute the targets checksum (ShardCtl::row_sum) the learned engine checks its index against;
+// with_posmap: also write the position map (when it is allocated).
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
-                              bool row_sum = false, bool permute = true);
+                              bool row_sum = false, bool permute = true, bool with_posmap = true);
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream);
 // Tries of the update pass's first wait for its staged bitmap; returns the previous value.
 uint32_t set_first_wait_limit(uint32_t tries);

@@ -764,7 +764,16 @@ namespace {
 // learned tick plans without the previous tick's features (no prediction, dense).
 __global__ void k_learn_resume(LearnCtl* c) { c->feat_done = 0; }
 
-constexpr uint32_t kGateMin = 4, kGateMax = 64;   // chunks on the plain graph after a dense-only probe
+constexpr uint32_t kGateChunks = 64;   // chunks on the plain graph after a dense-only probe, at most
+
+// What the gate reads back from the shard's control block around a chunk on
+// the plain graph: the statistics counters through slot_total.
+struct GateSnap {
+  unsigned long long before[11], after[11];
+};
+constexpr size_t kGateSnapOff = offsetof(ShardCtl, ctr);
+constexpr size_t kGateSnapBytes = offsetof(ShardCtl, slot_total) + sizeof(unsigned long long) - kGateSnapOff;
+static_assert(kGateSnapBytes == sizeof(GateSnap::before), "GateSnap mirrors ShardCtl::ctr .. slot_total");
 
 __global__ void k_learn_set_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopamine) {
   ctl->tick_base = tick_base;
@@ -807,12 +816,19 @@ struct Learned {
   uint32_t adam_step = 0;
   int32_t policy = -1;
   uint32_t collect = 0;
-  // gate: while the predictor keeps choosing the dense form, chunks run on a
-  // plain graph (no features, no plan); gate_len doubles after every probe that
-  // chose dense throughout (up to kGateMax chunks), back to kGateMin after one
-  // that chose sparse
-  uint32_t gate_left = 0, gate_len = 0;
+  // gate: after a chunk in which the predictor chose the dense form on every
+  // tick, up to kGateChunks chunks run on a plain graph (no features, no plan,
+  // no position map).  The plain graph's own exact counts end the gate early:
+  // each gated chunk's evaluated slots and hits are read back (two chunks
+  // behind, so the GPU never waits for the host), and a chunk in which the
+  // sparse form could have won sends the next chunk back to the predictor.
+  float ratio = 3.f;
+  uint32_t gate_left = 0;
   uint64_t gated_ticks = 0;
+  uint64_t chunk_no = 0;
+  GateSnap* h_gate = nullptr;       // pinned, two slots (chunk number & 1)
+  cudaEvent_t gate_ev[2] = {nullptr, nullptr};
+  bool gate_pend[2] = {false, false};
   const void* rows_base = nullptr;   // the row cache the graphs were captured with
   std::map<std::tuple<uint32_t, uint32_t>, cudaGraphExec_t> graphs;
   cudaStream_t capture = nullptr;
@@ -839,6 +855,9 @@ static void learned_free(Learned* L) {
   if (!L) return;
   L->drop_graphs();
   if (L->capture) cudaStreamDestroy(L->capture);
+  for (cudaEvent_t ev : L->gate_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (L->h_gate) cudaFreeHost(L->h_gate);
   void* ptrs[] = {L->base, L->inv, L->inv_seg, L->stage, L->partial};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1060,6 +1079,8 @@ int32_t axc_learned_create(const AxcLearnedDesc* d, void** out_handle) {
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->capture, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaHostAlloc(&L->h_gate, 2 * sizeof(GateSnap), cudaHostAllocDefault);
+  for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaEventCreateWithFlags(&L->gate_ev[q], cudaEventDisableTiming);
   if (e == cudaSuccess && ((size_t)T + 1) * 4 > 48 * 1024)
     e = cudaFuncSetAttribute(k_learn_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(((size_t)T + 1) * 4));
   if (e == cudaSuccess) e = learned_index(*L, nullptr);
@@ -1092,8 +1113,9 @@ int32_t axc_learned_set_policy(void* handle, int32_t policy, float ratio, float 
   hc.margin = margin;
   hc.slack = slack;
   L->policy = policy;
+  L->ratio = ratio;
   L->gate_left = 0;
-  L->gate_len = 0;
+  L->gate_pend[0] = L->gate_pend[1] = false;
   return (int32_t)cudaMemcpy(L->ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice);
 }
 
@@ -1152,7 +1174,9 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     }
     cudaError_t ce = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
     if (ce != cudaSuccess) return ce;
-    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true, true);
+    // the plain graph needs neither the index checksum nor the position map
+    // (every learned graph's own row copy writes both)
+    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, kind != 2, true, kind != 2);
     for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) {
       if (kind == 2) {   // the plain engine's tick on the staged bitmask rows
         TickArgs a{};
@@ -1184,6 +1208,21 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   const bool gate_on = L->policy < 0 && !L->collect;
   for (uint32_t c = 0; c < ticks / tpg && e == cudaSuccess; c++) {
     const uint32_t t0 = tick0 + c * tpg;
+    const uint32_t slot = (uint32_t)(L->chunk_no++ & 1u);
+    // the counts of the gated chunk two chunks back (its copies are done once
+    // the chunk before this one started): could the sparse form have won?
+    if (L->gate_pend[slot]) {
+      L->gate_pend[slot] = false;
+      e = cudaEventSynchronize(L->gate_ev[slot]);
+      if (e != cudaSuccess) break;
+      const GateSnap& g = L->h_gate[slot];
+      const double ev_slots = (double)(g.after[1] - g.before[1]), hit = (double)(g.after[2] - g.before[2]);
+      const double live = (double)g.after[10] * tpg;   // live slots x ticks: the active synapses scale with them
+      if (gate_on && L->gate_left > 0 && ev_slots > 0 && (double)L->ratio * hit * live < ev_slots * ev_slots) {
+        L->gate_left = 0;
+        k_learn_resume<<<1, 1, 0, st>>>(L->ctl);   // the features history is stale
+      }
+    }
     const bool gated = gate_on && L->gate_left > 0;
     cudaGraphExec_t exec = nullptr;
     e = graph_of(gated ? 2u : (features_on ? 1u : 0u), &exec);
@@ -1202,9 +1241,16 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     const size_t picked_at = offsetof(LearnCtl, stat) + kStSparsePicked * sizeof(unsigned long long);
     if (e == cudaSuccess && gate_on && !gated)
       e = cudaMemcpyAsync(&picked0, reinterpret_cast<char*>(L->ctl) + picked_at, 8, cudaMemcpyDeviceToHost, st);
+    const char* snap_src = reinterpret_cast<const char*>(s->ctl) + kGateSnapOff;
+    if (e == cudaSuccess && gated)
+      e = cudaMemcpyAsync(L->h_gate[slot].before, snap_src, kGateSnapBytes, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
     if (e != cudaSuccess) break;
     if (gated) {
+      e = cudaMemcpyAsync(L->h_gate[slot].after, snap_src, kGateSnapBytes, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaEventRecord(L->gate_ev[slot], st);
+      if (e != cudaSuccess) break;
+      L->gate_pend[slot] = true;
       L->gate_left--;
       L->gated_ticks += tpg;
       if (L->gate_left == 0) k_learn_resume<<<1, 1, 0, st>>>(L->ctl);   // the features history is stale
@@ -1215,12 +1261,7 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     e = cudaMemcpyAsync(&picked1, reinterpret_cast<char*>(L->ctl) + picked_at, 8, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) break;
-    if (picked1 == picked0) {
-      L->gate_len = L->gate_len ? std::min(2 * L->gate_len, kGateMax) : kGateMin;
-      L->gate_left = L->gate_len;
-    } else {
-      L->gate_len = 0;
-    }
+    if (picked1 == picked0) L->gate_left = kGateChunks;
   }
   return (int32_t)e;
 }

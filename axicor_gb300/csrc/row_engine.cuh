@@ -139,11 +139,15 @@ __device__ __forceinline__ void col_write(const ColWT& wt, uint32_t n, uint32_t 
 
 // The lit-sum form runs tick k when the rows' tested prefixes are short (at most
 // an eighth of the live slots: otherwise the 8-lane pass is faster) and every
-// axon the row layout took as fully lit is fully lit this tick.
+// axon the row layout took as fully lit is fully lit this tick.  Every thread
+// of both update kernels asks at its start; the three words were written by
+// earlier kernels and no kernel that asks writes them, so plain loads (cached
+// in L1 after the first warp of an SM) serve it: uncached loads sent every
+// warp's request to the one L2 slice that holds the control block, a few
+// microseconds per launch.
 __device__ __forceinline__ bool lsum_tick(const ShardCtl* ctl, uint32_t k) {
-  const unsigned long long p = *(volatile const unsigned long long*)&ctl->pfx_total;
-  const unsigned long long c = *(volatile const unsigned long long*)&ctl->slot_total;
-  return c > 0 && p * 8ull <= c && *(volatile const uint32_t*)&ctl->dense[k & 1] == 0u;
+  const unsigned long long p = ctl->pfx_total, c = ctl->slot_total;
+  return c > 0 && p * 8ull <= c && ctl->dense[k & 1] == 0u;
 }
 
 // Per-neuron GSOP constants (physics.cu:290-345).
@@ -1919,7 +1923,7 @@ void rows_free(ShardScratch& s) {
 }
 
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
-                              bool row_sum, bool permute) {
+                              bool row_sum, bool permute, bool with_posmap) {
   RowCache& r = *s.rows;
   k_rows_reset_lists<<<1, 1, 0, stream>>>(s.ctl);
   cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
@@ -1937,7 +1941,7 @@ cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t 
                                                     r.rw, r.cnt, r.amask, r.omask, r.lfz, s.ctl, A,
                                                     row_sum ? 1u : 0u, permute ? 1u : 0u,
                                                     permute ? r.xlit : nullptr, permute ? r.lsum : nullptr,
-                                                    r.posmap);
+                                                    with_posmap ? r.posmap : nullptr);
   }
   return cudaGetLastError();
 }

@@ -326,8 +326,14 @@ def run_gb300(args, dist: Dist) -> dict | None:
         kb = update_kernel_bytes(prof_ticks, ev, spk, lay.padded_n)
     elif names[top] == "gsop":
         kb = 8 * gs
-    elif names[top] in ("axons", "prologue"):
-        kb = prof_ticks * (64 * A_ + (8 if engine == 1 else 4) * A_ + (4 + 4) * lay.padded_n)
+    elif names[top] == "prologue":
+        # per axon: heads read and written (64), split masks written (8), owner count (4), pending pushes (4);
+        # per neuron: timer read (1), and for the refractory ones timer written and flags read and written (3);
+        # per evaluated neuron its list entry (4); per spiker its pending-push count cleared (4)
+        Np_ = lay.padded_n
+        kb = prof_ticks * (80 * A_ + Np_) + 3 * (prof_ticks * Np_ - nev) + 4 * nev + 4 * spk
+    elif names[top] == "axons":
+        kb = prof_ticks * (64 * A_ + 4 * A_ + (4 + 4) * lay.padded_n)
     else:
         kb = 68 * spk
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}

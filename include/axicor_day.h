@@ -522,11 +522,13 @@ int32_t axc_learned_samples(void* handle, uint32_t first, uint32_t count, float*
  * ticks, [9] ticks run with the predictor gated off, [12] recorded pairs,
  * [13] feature history length, [14] tiles, [15] index capacity.
  * Gate (policy -1, not collecting): a chunk of ticks_per_graph ticks in which
- * the predictor chose the dense form on every tick is followed by 4 chunks on
- * the plain engine's graph (no features, no plan), then a probe chunk with the
- * predictor; each dense-only probe doubles the gate (up to 64 chunks), a probe
- * that chose the sparse form ends it.  Dense ticks of both graphs run the
- * plain engine's passes, so the state is the same either way. */
+ * the predictor chose the dense form on every tick is followed by up to 64
+ * chunks on the plain engine's graph (no features, no plan), then a probe
+ * chunk with the predictor.  The gate ends early when a gated chunk's exact
+ * counts say the sparse form could have won (ratio x hits x live slots <
+ * evaluated slots squared, over the chunk); those counts are read back two
+ * chunks behind, so the host never stalls the stream.  Dense ticks of both
+ * graphs run the plain engine's passes, so the state is the same either way. */
 int32_t axc_learned_stats(void* handle, uint64_t out[16]);
 int32_t axc_learned_reset_stats(void* handle);
 void axc_learned_destroy(void* handle);

@@ -213,3 +213,29 @@ def test_learned_schedule_faster_than_plain_on_quiet_brain(gpu):
     finally:
         b.close()
         plain.free()
+
+
+def test_gate_follows_the_brain_from_dense_to_sparse(gpu):
+    """Policy -1 on a brain that bursts (ticks 20..100: up to 14 % of the neurons spike per tick) and then goes
+    quiet: while it bursts the predictor chooses the dense form for a whole chunk, so the gate puts the next
+    chunks on the plain graph; once the brain is quiet the plain graph's own exact counts end the gate (well
+    before its 64-chunk limit) and the predictor runs sparse ticks again.  Bit-exact against the oracle."""
+    ticks, tpg = 800, 20
+    b = LBrain(brain("quiet", dims=(32, 32, 16), slots=64, ticks=ticks), ticks)
+    try:
+        b.eng.set_params(np.zeros(L.param_count(), np.float32))   # residual on the last tick: the last-tick rule
+        b.eng.set_policy(L.Policy(policy=-1))
+        hist = []
+        for t in range(0, ticks, tpg):
+            b.eng.run(t, tpg, tpg)
+            st = b.eng.stats()
+            hist.append((st["gated_ticks"], st["sparse_ticks"]))
+        gated = [i for i in range(len(hist)) if hist[i][0] > (hist[i - 1][0] if i else 0)]
+        assert gated, hist
+        first, last = gated[0], gated[-1]
+        assert last - first + 1 < 64, hist
+        later_sparse = hist[-1][1] - hist[last][1]
+        assert later_sparse > 0, ("no sparse tick after the gate ended", hist)
+        b.check(*b.oracle(ticks), "gated and ungated chunks")
+    finally:
+        b.close()
