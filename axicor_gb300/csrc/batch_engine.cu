@@ -13,6 +13,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <map>
 #include <mutex>
@@ -44,9 +45,13 @@ struct GraphCache {
   cudaStream_t capture = nullptr;
 };
 
-__global__ void k_set_batch_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopamine) {
+// Per batch, before its graph: the tick base and dopamine the captured kernels
+// read, and (row engine) whether the batch lays its row copy out anew.
+__global__ void k_set_batch_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopamine, uint32_t rows, uint32_t force,
+                                uint32_t ticks) {
   ctl->tick_base = tick_base;
   ctl->dopamine = dopamine;
+  if (rows) layout_decide(ctl, force, ticks);
 }
 
 cudaError_t ensure_counts(ShardScratch& s, uint32_t batch, bool* realloc, cudaStream_t stream) {
@@ -109,7 +114,7 @@ cudaError_t batch_prepare(const BatchArgs& b, ShardScratch** out_s, uint32_t* ou
   cudaError_t e;
   ShardScratch* s = scratch_for(b.vram, b.padded_n, b.total_axons, &e);
   if (!s) return e;
-  rows_touched(*s);   // the batch's row copy replaces the per-tick entry point's
+  s->tick_rows_valid.store(false);   // the batch's row copy replaces the per-tick entry point's
   // Captured graphs hold the addresses of the scratch buffers: any
   // reallocation below drops them.
   bool realloc = false;
@@ -123,6 +128,10 @@ cudaError_t batch_prepare(const BatchArgs& b, ShardScratch** out_s, uint32_t* ou
     realloc = realloc || (before != nullptr && before != s->rows->base);
   }
   if (realloc) graph_cache_drop(s);
+  // the device decides whether the batch lays the rows out anew or keeps the
+  // last batch's copy (written back, so it matches the .state blob); a copy
+  // that something invalidated is laid out anew for sure
+  const bool force = rows ? batch_rows_force(*s) : true;
 
   // bulk H2D of the batch's inputs (shard.rs:54-68)
   const AxcIoBuffers* io = b.io;
@@ -140,7 +149,7 @@ cudaError_t batch_prepare(const BatchArgs& b, ShardScratch** out_s, uint32_t* ou
   else
     e = cudaMemsetAsync(s->batch_counts, 0, (size_t)b.ticks * 4, stream);
   if (e != cudaSuccess) return e;
-  k_set_batch_ctl<<<1, 1, 0, stream>>>(s->ctl, b.tick_base, (int32_t)b.dopamine);
+  k_set_batch_ctl<<<1, 1, 0, stream>>>(s->ctl, b.tick_base, (int32_t)b.dopamine, rows, force ? 1u : 0u, b.ticks);
   // burst-counter reset before the batch (shard.rs:71)
   e = launch_reset_burst(*b.vram, b.padded_n, stream);
   if (e != cudaSuccess) return e;
@@ -155,7 +164,8 @@ cudaError_t batch_prepare(const BatchArgs& b, ShardScratch** out_s, uint32_t* ou
 cudaError_t batch_capture(const BatchArgs& b, ShardScratch& s, uint32_t rows, uint32_t fix_cap, cudaStream_t cap) {
   const AxcIoBuffers* io = b.io;
   const uint32_t words = io->input_words_per_tick;
-  cudaError_t le = rows ? launch_rows_begin(*b.vram, s, b.padded_n, b.total_axons, cap) : cudaSuccess;
+  cudaError_t le = cudaSuccess;
+  if (rows) le = launch_rows_begin(*b.vram, s, b.padded_n, b.total_axons, cap, false, true, true, true);
   for (uint32_t k = 0; k < b.ticks && le == cudaSuccess; k++) {
     TickArgs a{};
     a.padded_n = b.padded_n;
@@ -269,7 +279,7 @@ extern "C" int32_t axc_profile_ticks(const ShardVramPtrs* vram, uint32_t padded_
       old->execs.clear();
     }
     cudaMemsetAsync(s->batch_counts, 0, (size_t)ticks * 4, st);
-    k_set_batch_ctl<<<1, 1, 0, st>>>(s->ctl, tick0, (int32_t)dopamine);
+    k_set_batch_ctl<<<1, 1, 0, st>>>(s->ctl, tick0, (int32_t)dopamine, 0u, 1u, ticks);   // layouts its own
     e = launch_rows_begin(*vram, *s, padded_n, total_axons, st);
     if (e != cudaSuccess) return (int32_t)e;
   }

@@ -47,6 +47,10 @@ struct ShardCtl {
   uint32_t dense[2];      // row engine: tick k (slot k & 1) has an axon off the lit set the row layout assumed
   unsigned long long pfx_total;   // row engine: slots outside the frozen lit-sum part of the rows (batch start)
   unsigned long long slot_total;  // row engine: live slots of the rows (batch start)
+  uint32_t lay_now;       // row engine: this batch lays the row copy out anew (layout_decide)
+  uint32_t lay_since;     // row engine: ticks since the last layout
+  uint32_t lay_every;     // row engine: ticks between layouts while the lit-sum criterion holds
+  uint32_t pad3;
 };
 
 // Neuron-major copy of the dendrites used by the batch engine for the length
@@ -99,7 +103,52 @@ struct ShardScratch {
   uint32_t tick_since_build = 0;        // per-tick calls since the row copy was laid out
   const void* state_base = nullptr;     // the shard's .state allocation (invalidation by address)
   size_t state_bytes = 0;
+  // Batch path: the row copy (layout, weights, lit-sum sums) is kept from one
+  // batch to the next while it matches the shard's memory and the LUT (the
+  // device decides each batch whether to lay it out anew: layout_decide).
+  // Cleared by every route that clears tick_rows_valid, and by the per-tick
+  // entry point; the next batch then lays the rows out for sure.
+  std::atomic<bool> batch_rows_valid{false};
+  uint64_t batch_rows_lut = 0;           // LUT generation of the batch layout
 };
+
+constexpr uint32_t kBatchRelayoutMin = 100, kBatchRelayoutMax = 1600;   // ticks between batch layouts
+
+uint64_t lut_generation();
+
+// Whether the next batch must lay the row copy out anew whatever the device
+// decides (the kept copy is stale or from another LUT); marks the copy the
+// batch leaves as valid.
+inline bool batch_rows_force(ShardScratch& s) {
+  const uint64_t gen = lut_generation();
+  const bool force = !(s.batch_rows_valid.load() && s.batch_rows_lut == gen);
+  s.batch_rows_lut = gen;
+  s.batch_rows_valid.store(true);
+  return force;
+}
+
+#ifdef __CUDACC__
+// The device's layout decision for the next `ticks` ticks of a batch (one
+// thread, before the batch): a new layout when forced, while the current one
+// misses the lit-sum criterion (at most an eighth of the live slots outside
+// the lit-sum groups: the weights are still freezing, or the axons taken as
+// fully lit were not yet), and otherwise every lay_every ticks, doubling from
+// kBatchRelayoutMin to kBatchRelayoutMax.  The layout kernels of the batch
+// return at once when lay_now is 0.
+__device__ __forceinline__ void layout_decide(ShardCtl* c, uint32_t force, uint32_t ticks) {
+  const bool met = c->slot_total > 0 && c->pfx_total * 8ull <= c->slot_total;
+  const bool build = force || !met || c->lay_since >= c->lay_every;
+  if (build) {
+    const uint32_t twice = 2u * c->lay_every;
+    c->lay_every = (force || !met || c->lay_every < kBatchRelayoutMin) ? kBatchRelayoutMin
+                   : twice < kBatchRelayoutMax                          ? twice
+                                                                        : kBatchRelayoutMax;
+    c->lay_since = 0;
+  }
+  c->lay_since += ticks;
+  c->lay_now = build ? 1u : 0u;
+}
+#endif
 
 constexpr uint32_t kFixCap = 1u << 22;  // deferred GSOP slots per tick before the rescan path
 constexpr uint32_t kMaxUpdateWarps = 32u * 1024u;  // warps of the update pass (32 per SM)
@@ -113,10 +162,14 @@ void rows_free(ShardScratch& s);
 // written by every later row copy of the shard that asks for it.
 cudaError_t rows_posmap(ShardScratch& s, cudaStream_t stream);
 // row_sum: also compute the targets checksum (ShardCtl::row_sum) the learned engine checks its index against;
-// with_posmap: also write the position map (when it is allocated).
+// with_posmap: also write the position map (when it is allocated); conditional: the layout kernels lay
+// the rows out only when the device's decision (ShardCtl::lay_now, layout_decide) says so, and
+// otherwise keep the copy (only the per-tick lists are reset).
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
-                              bool row_sum = false, bool permute = true, bool with_posmap = true);
+                              bool row_sum = false, bool permute = true, bool with_posmap = true,
+                              bool conditional = false);
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream);
+
 // Tries of the update pass's first wait for its staged bitmap; returns the previous value.
 uint32_t set_first_wait_limit(uint32_t tries);
 
@@ -129,8 +182,11 @@ void graph_cache_free(ShardScratch* s);  // batch_engine.cu
 void graph_cache_drop(ShardScratch* s);  // batch_engine.cu: destroys the captured graphs only
 uint32_t fix_capacity();                 // batch_engine.cu: deferred-GSOP list capacity in use
 
-// The per-tick row cache of a shard no longer matches its memory (shard_api.cu).
-inline void rows_touched(ShardScratch& s) { s.tick_rows_valid.store(false); }
+// The row caches of a shard (per-tick and batch) no longer match its memory (shard_api.cu).
+inline void rows_touched(ShardScratch& s) {
+  s.tick_rows_valid.store(false);
+  s.batch_rows_valid.store(false);
+}
 // Marks every shard whose .state allocation overlaps [dst, dst + size).
 void invalidate_overlapping(const void* dst, size_t size);
 // Looks up a shard's scratch without creating it (nullptr if none).

@@ -65,6 +65,88 @@ __device__ __forceinline__ float warp_sum_f(float v) {
   return v;
 }
 
+// D = A x B + D on the tensor cores: A 16x16 BF16 (row-major), B 16x8 BF16
+// (column-major), D 16x8 FP32 (PTX mma.sync.aligned.m16n8k16.row.col, BF16
+// inputs, FP32 accumulation).  Fragments of lane l, g = l / 4, q = l % 4:
+// a[0] row g cols 2q, 2q+1; a[1] row g + 8; a[2] row g cols 2q + 8, 2q + 9;
+// a[3] row g + 8 cols 2q + 8, 2q + 9; b[0] rows (k) 2q, 2q+1 of column g;
+// b[1] rows 2q + 8, 2q + 9; d[0], d[1] row g cols 2q, 2q+1; d[2], d[3] row g + 8.
+// The lower-indexed element of a pair sits in the low half of its register.
+__device__ __forceinline__ void mma_bf16_16816(float d[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ uint32_t ld_bf16x2(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// The MLP on 16 input rows by one warp (all 32 lanes): the hidden layer as 64
+// tensor-core MMAs (16 tiles of 8 units x 4 steps of 16 features, BF16 inputs
+// and weights, FP32 accumulators starting at b1), ReLU, BF16 rounding of the
+// activations, then the output layer in FP32 in a fixed order: each lane sums
+// w2[u] * h over its units (tile by tile, unit 2q before 2q + 1), then the
+// four lanes of a quad are added pairwise (xor 1, then xor 2).  a_frag holds
+// the rows' A fragments (mlp_a_frags); *yg / *yg8: the sums for rows g and
+// g + 8, the same on the four lanes of the quad, without b2 and the residual.
+__device__ __forceinline__ void mlp_warp16(const __nv_bfloat16* __restrict__ wb, const uint32_t (&a_frag)[4][4],
+                                           float* yg, float* yg8, float (*keep_a)[4] = nullptr) {
+  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
+  float sg = 0.f, sg8 = 0.f;
+#pragma unroll 4
+  for (int nt = 0; nt < (int)(kHid / 8); nt++) {
+    const uint32_t u0 = 8u * nt + 2u * q;
+    const float b1a = __bfloat162float(wb[kOffB1 + u0]), b1b = __bfloat162float(wb[kOffB1 + u0 + 1]);
+    float d[4] = {b1a, b1b, b1a, b1b};
+    const __nv_bfloat16* wrow = wb + (size_t)(8u * nt + g) * kFeat + 2u * q;
+#pragma unroll
+    for (int ks = 0; ks < 4; ks++) mma_bf16_16816(d, a_frag[ks], ld_bf16x2(wrow + 16 * ks), ld_bf16x2(wrow + 16 * ks + 8));
+    if (keep_a) {
+#pragma unroll
+      for (int e = 0; e < 4; e++) keep_a[nt][e] = d[e];
+    }
+    const float w2a = __bfloat162float(wb[kOffW2 + u0]), w2b = __bfloat162float(wb[kOffW2 + u0 + 1]);
+    sg = __fadd_rn(sg, __fmul_rn(w2a, bf16r(fmaxf(d[0], 0.f))));
+    sg = __fadd_rn(sg, __fmul_rn(w2b, bf16r(fmaxf(d[1], 0.f))));
+    sg8 = __fadd_rn(sg8, __fmul_rn(w2a, bf16r(fmaxf(d[2], 0.f))));
+    sg8 = __fadd_rn(sg8, __fmul_rn(w2b, bf16r(fmaxf(d[3], 0.f))));
+  }
+  sg = __fadd_rn(sg, __shfl_xor_sync(kFull, sg, 1));
+  sg = __fadd_rn(sg, __shfl_xor_sync(kFull, sg, 2));
+  sg8 = __fadd_rn(sg8, __shfl_xor_sync(kFull, sg8, 1));
+  sg8 = __fadd_rn(sg8, __shfl_xor_sync(kFull, sg8, 2));
+  *yg = sg;
+  *yg8 = sg8;
+}
+
+// A fragments of 16 rows of FP32 features (row r at x + r * kFeat; rows >=
+// nrows are zero), rounded to BF16.
+__device__ __forceinline__ void mlp_a_frags(const float* __restrict__ x, uint32_t nrows, uint32_t (&a)[4][4]) {
+  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
+  const bool vg = g < nrows, vg8 = g + 8u < nrows;
+  const float* xg = x + (size_t)g * kFeat + 2u * q;
+  const float* xg8 = x + (size_t)(g + 8u) * kFeat + 2u * q;
+#pragma unroll
+  for (int ks = 0; ks < 4; ks++) {
+    const int c = 16 * ks;
+    a[ks][0] = vg ? pack_bf16x2(xg[c], xg[c + 1]) : 0u;
+    a[ks][1] = vg8 ? pack_bf16x2(xg8[c], xg8[c + 1]) : 0u;
+    a[ks][2] = vg ? pack_bf16x2(xg[c + 8], xg[c + 9]) : 0u;
+    a[ks][3] = vg8 ? pack_bf16x2(xg8[c + 8], xg8[c + 9]) : 0u;
+  }
+}
+
+// The MLP's output for row r of x given the quad sum s of mlp_warp16:
+// (s + b2) + x[r][kResidF] (the residual input, BF16-rounded like the rest).
+__device__ __forceinline__ float mlp_out(const __nv_bfloat16* __restrict__ wb, float s, const float* xr) {
+  return __fadd_rn(__fadd_rn(s, __bfloat162float(wb[kOffB2])), bf16r(xr[kResidF]));
+}
+
 // One hidden unit u of the MLP on the BF16-rounded input xs (shared memory):
 // returns the pre-activation (FP32, k = 0..63 in order).
 __device__ __forceinline__ float mlp_unit(const __nv_bfloat16* __restrict__ wb, uint32_t u, const float* xs) {
@@ -775,9 +857,12 @@ constexpr size_t kGateSnapOff = offsetof(ShardCtl, ctr);
 constexpr size_t kGateSnapBytes = offsetof(ShardCtl, slot_total) + sizeof(unsigned long long) - kGateSnapOff;
 static_assert(kGateSnapBytes == sizeof(GateSnap::before), "GateSnap mirrors ShardCtl::ctr .. slot_total");
 
-__global__ void k_learn_set_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopamine) {
+// Per chunk, before its graph: tick base, dopamine, and whether the chunk lays
+// its rows out anew (always on learned chunks: force).
+__global__ void k_learn_set_ctl(ShardCtl* ctl, uint32_t tick_base, int32_t dopamine, uint32_t force, uint32_t ticks) {
   ctl->tick_base = tick_base;
   ctl->dopamine = dopamine;
+  layout_decide(ctl, force, ticks);
 }
 
 // splitmix64: seeded parameter init and minibatch order, identical on every host.
@@ -1149,7 +1234,7 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
   e = rows_alloc(*s, L->N, L->A, true, st);
   if (e == cudaSuccess) e = rows_posmap(*s, st);
   if (e != cudaSuccess) return (int32_t)e;
-  rows_touched(*s);
+  s->tick_rows_valid.store(false);   // this run's rows replace the per-tick entry point's
   if (L->rows_base != s->rows->base) {
     L->drop_graphs();
     L->rows_base = s->rows->base;
@@ -1164,7 +1249,8 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     L->drop_graphs();
   }
   const bool features_on = L->policy < 0 || L->collect;
-  // graph kinds: 0/1 learned (features off/on), 2 plain (the gate)
+  // graph kinds: 0/1 learned (features off/on), 2 plain (the gate); the row
+  // layout of each chunk follows the device's decision (layout_decide)
   auto graph_of = [&](uint32_t kind, cudaGraphExec_t* out) -> cudaError_t {
     const auto key = std::make_tuple(tpg, kind);
     auto it = L->graphs.find(key);
@@ -1174,9 +1260,9 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
     }
     cudaError_t ce = cudaStreamBeginCapture(L->capture, cudaStreamCaptureModeThreadLocal);
     if (ce != cudaSuccess) return ce;
-    // the plain graph needs neither the index checksum nor the position map
-    // (every learned graph's own row copy writes both)
-    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, kind != 2, true, kind != 2);
+    // every layout of this engine writes the index checksum and the position
+    // map (the sparse form reads the rows through it), when the device lays out
+    cudaError_t le = launch_rows_begin(L->v, *s, L->N, L->A, L->capture, true, true, true, true);
     for (uint32_t k = 0; k < tpg && le == cudaSuccess; k++) {
       if (kind == 2) {   // the plain engine's tick on the staged bitmask rows
         TickArgs a{};
@@ -1224,6 +1310,10 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
       }
     }
     const bool gated = gate_on && L->gate_left > 0;
+    // the first chunk of a call lays the rows out (another path may have laid
+    // them out without the position map since); later chunks keep them as the
+    // batch path does
+    const bool force = batch_rows_force(*s) || c == 0;
     cudaGraphExec_t exec = nullptr;
     e = graph_of(gated ? 2u : (features_on ? 1u : 0u), &exec);
     if (e != cudaSuccess) break;
@@ -1235,7 +1325,7 @@ int32_t axc_learned_run(void* handle, uint32_t tick0, uint32_t ticks, uint32_t t
         e = cudaMemsetAsync(L->stage + (size_t)have * L->words, 0, (size_t)(tpg + 1 - have) * L->words * 4, st);
       if (e != cudaSuccess) break;
     }
-    k_learn_set_ctl<<<1, 1, 0, st>>>(s->ctl, L->tick_base + t0, (int32_t)L->dopamine);
+    k_learn_set_ctl<<<1, 1, 0, st>>>(s->ctl, L->tick_base + t0, (int32_t)L->dopamine, force ? 1u : 0u, tpg);
     e = launch_reset_burst(L->v, L->N, st);
     unsigned long long picked0 = 0, picked1 = 0;
     const size_t picked_at = offsetof(LearnCtl, stat) + kStSparsePicked * sizeof(unsigned long long);

@@ -456,7 +456,9 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
                                                     uint4* __restrict__ omask, uint8_t* __restrict__ lfz,
                                                     ShardCtl* __restrict__ ctl, uint32_t A, uint32_t want_sum,
                                                     uint32_t permute, const uint32_t* __restrict__ xlit,
-                                                    int2* __restrict__ lsum, uint8_t* __restrict__ posmap) {
+                                                    int2* __restrict__ lsum, uint8_t* __restrict__ posmap,
+                                                    uint32_t cond) {
+  if (cond && !ctl->lay_now) return;   // the batch keeps the last layout
   __shared__ uint32_t s_t[AXC_MAX_DENDRITES][33];
   __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
   __shared__ uint32_t s_cnt[32];
@@ -523,9 +525,25 @@ __global__ void __launch_bounds__(256) k_rows_build(const uint32_t* __restrict__
   }
 }
 
+// Layout start: the owner counts cleared and, for permuted rows, the axons
+// fully lit in the last tick the rows saw (the lit bitmap it left) taken as
+// the lit set of the layout (the prologue checks every tick that they still
+// are).
+__global__ void __launch_bounds__(256) k_rows_prep(const ShardCtl* __restrict__ ctl, uint32_t* __restrict__ mult,
+                                                   uint32_t A, const uint32_t* __restrict__ lit,
+                                                   uint32_t* __restrict__ xlit, uint32_t cond) {
+  if (cond && !ctl->lay_now) return;
+  const uint32_t words = A / 32 + 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < A; i += gridDim.x * blockDim.x) {
+    mult[i] = 0u;
+    if (xlit && i < words) xlit[i] = lit[i];
+  }
+}
+
 __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ s2a, uint32_t N, uint32_t A,
                                                    uint32_t* __restrict__ mult, uint2* __restrict__ mask2,
-                                                   ShardCtl* __restrict__ ctl) {
+                                                   ShardCtl* __restrict__ ctl, uint32_t cond) {
+  if (cond && !ctl->lay_now) return;
   const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n == 0) {
     mask2[A] = make_uint2(0u, 0x80000000u);   // dummy entry of invalid targets: no hit, exact path
@@ -1215,6 +1233,28 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   block_count(gdone, nev, 0, &ctl->ctr[4]);
 }
 
+// Sums six per-thread counters over a 256-thread block into ctr[1..5] and
+// ctr[7] (evaluated slots, hits, spikes, GSOP slots, evaluated neurons, tested
+// slots): one barrier, one atomic per counter.
+__device__ __forceinline__ void block_count256(uint32_t a1, uint32_t a2, uint32_t a3, uint32_t a4, uint32_t a5,
+                                               uint32_t a7, unsigned long long* ctr) {
+  __shared__ uint32_t red[6][8];
+  const uint32_t v[6] = {__reduce_add_sync(kFull, a1), __reduce_add_sync(kFull, a2), __reduce_add_sync(kFull, a3),
+                         __reduce_add_sync(kFull, a4), __reduce_add_sync(kFull, a5), __reduce_add_sync(kFull, a7)};
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int c = 0; c < 6; c++) red[c][w] = v[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    unsigned long long sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) sum += red[threadIdx.x][q];
+    if (sum) atomicAdd(ctr + (threadIdx.x == 5 ? 7 : threadIdx.x + 1), sum);
+  }
+}
+
 // The hit test of one slot as the 8-lane pass makes it (row_slots): the
 // fully-lit shortcut for segments 1..seg_hi of variants whose length is the LUT
 // maximum (<= 16), else the tick's split masks and, where they do not decide,
@@ -1265,6 +1305,8 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
   if (!lsum_tick(ctl, k)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ctr[6] += 1;   // ticks on the lit-sum form
+  const uint32_t ecount = ctl->eval_count[k & 1];
+  if (blockIdx.x * blockDim.x >= ecount) return;   // no neuron for this block: no table to build
   __shared__ VariantParameters lut[16];
   __shared__ int2 gtab[16][16];
   __shared__ uint32_t s_pmax;
@@ -1275,7 +1317,6 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
   build_gtab(gtab, lut, dopamine);
   __syncthreads();
   const uint32_t tick = ctl->tick_base + k;
-  const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t seg_hi = min(ctl->seg_max, 30u);
   uint32_t ev_slots = 0, hits = 0, nspk = 0, gdone = 0, nev = 0, err = 0, tested = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ecount; i += gridDim.x * blockDim.x) {
@@ -1299,6 +1340,8 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
     int16_t* rw_n = rw + (size_t)n * kRowStride;
     int32_t i_in = ls.x;
     uint32_t h = c - pfx;   // the lit-sum slots are hits
+    // the tests of row positions 0..31 (the movable slots come first), kept for GSOP
+    uint32_t hit_bits = 0, fast_bits = 0;
     for (uint32_t q = 0; q < pfx; q += 4) {
       const uint4 T4 = *reinterpret_cast<const uint4*>(rt_n + q);
       const uint2 W4 = *reinterpret_cast<const uint2*>(rw_n + q);
@@ -1306,10 +1349,14 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
       for (int j = 0; j < 4; j++) {
         if (q + j >= pfx) break;
         bool fast;
-        if (slot_hit(word_of(T4, j), exact, gfast, prop, seg_hi, lit_bits, mask2, P.axon_heads, A, &fast)) {
+        const bool hit = slot_hit(word_of(T4, j), exact, gfast, prop, seg_hi, lit_bits, mask2, P.axon_heads, A, &fast);
+        if (hit) {
           i_in = wadd(i_in, (int32_t)half_of(W4, j));
           h++;
         }
+        const uint32_t bit = (q + j < 32u) ? (1u << (q + j)) : 0u;
+        hit_bits |= hit ? bit : 0u;
+        fast_bits |= fast ? bit : 0u;
       }
     }
     ev_slots += c;
@@ -1330,10 +1377,14 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
     // GSOP (physics.cu:281-373) of the movable slots; the frozen ones are left as they are
     gdone += c - lf;
     for (uint32_t q = 0; q < lf; q++) {
-      const uint32_t t = rt_n[q];
       const int16_t w16 = rw_n[q];
-      bool fast;
-      const bool hit = slot_hit(t, exact, gfast, prop, seg_hi, lit_bits, mask2, P.axon_heads, A, &fast);
+      bool fast, hit;
+      if (q < 32u) {   // tested in the prefix loop (lf <= pfx)
+        hit = (hit_bits >> q) & 1u;
+        fast = (fast_bits >> q) & 1u;
+      } else {
+        hit = slot_hit(rt_n[q], exact, gfast, prop, seg_hi, lit_bits, mask2, P.axon_heads, A, &fast);
+      }
       int16_t nw = w16;
       if (fast) {
         const int32_t aw = w16 < 0 ? -(int32_t)w16 : (int32_t)w16;
@@ -1343,6 +1394,7 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
         nw = (int16_t)(w16 < 0 ? -na : na);
         gdone++;
       } else {
+        const uint32_t t = rt_n[q];
         const int r = gsop_general(P.axon_heads, mask2, A, (t & AXC_TARGET_AXON_MASK) - 1u, t >> AXC_TARGET_SEG_SHIFT,
                                    p, flags, dopamine, &nw);
         if (r == 2) continue;
@@ -1362,9 +1414,7 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
   }
   const uint32_t err_any = __reduce_or_sync(kFull, err);
   if (err_any && (threadIdx.x & 31) == 0) atomicOr(&ctl->err, err_any);
-  block_count(ev_slots, hits, nspk, &ctl->ctr[1]);
-  block_count(gdone, nev, 0, &ctl->ctr[4]);
-  block_count(tested, 0, 0, &ctl->ctr[7]);
+  block_count256(ev_slots, hits, nspk, gdone, nev, tested, ctl->ctr);
 }
 
 // ---------------------------------------------------------------------------
@@ -1923,25 +1973,19 @@ void rows_free(ShardScratch& s) {
 }
 
 cudaError_t launch_rows_begin(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, cudaStream_t stream,
-                              bool row_sum, bool permute, bool with_posmap) {
+                              bool row_sum, bool permute, bool with_posmap, bool conditional) {
   RowCache& r = *s.rows;
+  const uint32_t cond = conditional ? 1u : 0u;
   k_rows_reset_lists<<<1, 1, 0, stream>>>(s.ctl);
-  cudaError_t e = cudaMemsetAsync(r.mult, 0, (size_t)A * 4, stream);
-  if (e != cudaSuccess) return e;
-  // the lit-sum part of the rows (permuted rows only): the axons fully lit in
-  // the last tick the rows saw (the lit bitmap it left) are taken as lit; the
-  // prologue checks every tick that they still are
-  if (permute) {
-    e = cudaMemcpyAsync(r.xlit, r.lit, ((size_t)A / 32 + 1) * 4, cudaMemcpyDeviceToDevice, stream);
-    if (e != cudaSuccess) return e;
-  }
+  if (A) k_rows_prep<<<std::min((A + 255) / 256, 4u * (uint32_t)sm_count()), 256, 0, stream>>>(
+             s.ctl, r.mult, A, r.lit, permute ? r.xlit : nullptr, cond);
   if (N) {
-    k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl);
+    k_rows_mult<<<(N + 255) / 256, 256, 0, stream>>>(v.soma_to_axon, N, A, r.mult, r.mask2, s.ctl, cond);
     k_rows_build<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_targets, v.dendrite_weights, v.soma_flags, N, r.rt,
                                                     r.rw, r.cnt, r.amask, r.omask, r.lfz, s.ctl, A,
                                                     row_sum ? 1u : 0u, permute ? 1u : 0u,
                                                     permute ? r.xlit : nullptr, permute ? r.lsum : nullptr,
-                                                    with_posmap ? r.posmap : nullptr);
+                                                    with_posmap ? r.posmap : nullptr, cond);
   }
   return cudaGetLastError();
 }

@@ -91,7 +91,7 @@ ShardScratch* scratch_for(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
     if (s->padded_n >= padded_n && s->total_axons >= total_axons) {
       if (s->state_base != vram->soma_voltage) {   // the same heads with another state allocation
         s->state_base = vram->soma_voltage;
-        s->tick_rows_valid.store(false);
+        rows_touched(*s);
       }
       return s;
     }
@@ -121,7 +121,7 @@ void invalidate_overlapping(const void* dst, size_t size) {
   for (auto& kv : registry()) {
     ShardScratch* s = kv.second;
     const uintptr_t b = reinterpret_cast<uintptr_t>(s->state_base);
-    if (b && lo < b + s->state_bytes && b < hi) s->tick_rows_valid.store(false);
+    if (b && lo < b + s->state_bytes && b < hi) rows_touched(*s);
   }
 }
 
@@ -281,6 +281,7 @@ int32_t cu_step_day_phase(const ShardVramPtrs* vram, uint32_t padded_n, uint32_t
     }
   }
   if (rows) {
+    s->batch_rows_valid.store(false);   // the batch path lays its rows out anew after per-tick calls
     const uint64_t gen = lut_generation();
     if (!s->tick_rows_valid.load() || s->tick_rows_lut != gen || s->tick_since_build >= kTickRelayout) {
       err = launch_rows_begin(*vram, *s, padded_n, total_axons, st);

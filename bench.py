@@ -251,12 +251,14 @@ def run_gb300(args, dist: Dist) -> dict | None:
     dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
+    torch.cuda.nvtx.range_push("timed")   # ncu --nvtx --nvtx-include "timed/" selects these launches
     ev0.record(stream)
     for _ in range(K):
         step_device(tick)
         tick += B
     ev1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     dist.barrier()
     ms = ev0.elapsed_time(ev1)
@@ -430,10 +432,12 @@ def per_tick_leg(r, t0=500, ticks=100, lead=10) -> dict:
         engine_ticks(start, t0)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("per_tick")   # ncu --nvtx --nvtx-include "per_tick/"
         e0.record(stream)
         engine_ticks(t0, t0 + ticks)
         e1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         ours_s = e0.elapsed_time(e1) / 1e3
         d_ours = digest(vram)
         # the batch path over the same ticks from the same state
@@ -593,10 +597,12 @@ def run_population(args) -> None:
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = Clocks(0)
     clocks.start()
+    torch.cuda.nvtx.range_push("timed")
     e0.record()
     pop.run(warm, ticks, tpg)
     e1.record()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     pop_s = e0.elapsed_time(e1) / 1e3
     ctr = pop.counters()
@@ -725,7 +731,9 @@ def run_learned(args) -> None:
     ticks = total - trace - window
     clocks = Clocks(0)
     clocks.start()
+    torch.cuda.nvtx.range_push("timed")
     t_learned = timed(lambda: eng.run(t1, ticks, tpg), default)
+    torch.cuda.nvtx.range_pop()
     t_plain = timed(lambda: plain_run(t1, ticks), ps)
     clk = clocks.stop()
     st = eng.stats()

@@ -244,7 +244,14 @@ int32_t axc_last_spikes(const ShardVramPtrs* vram, uint32_t* out_count, uint32_t
  * inputs (bitmask words_per_tick x batch, spike schedule max_spikes x batch)
  * into the device I/O buffers, resets the burst counters, then runs
  * `batch` ticks with global tick = tick_base + k.  The tick loop is captured
- * once into a CUDA graph per (shard, batch shape) and replayed.
+ * once into a CUDA graph per (shard, batch shape) and replayed.  The
+ * neuron-major row copy the ticks run on is kept from one batch to the next
+ * (its weights are written back to the .state blob at the end of every
+ * batch) and laid out anew at the second batch, then after 100, 200, 400,
+ * ... up to every 1,600 ticks, and whenever the shard's memory or the LUT
+ * may have changed (followed again by one at the next batch): after any
+ * entry point of this library that writes them, per-tick calls, and
+ * axc_shard_invalidate.
  * h_output_history, when not NULL, receives num_outputs x batch bytes
  * (device to host on the stream).  h_spike_counts may be NULL (no network
  * spikes).  Asynchronous on `stream` unless h_output_history is given, in
@@ -366,8 +373,10 @@ int32_t axc_tick_engine_mode(int32_t mode);
 
 /* No counterpart in the reference.  A caller that writes a shard's targets,
  * weights, flags or soma_to_axon by other means than this library (its own
- * kernels, a raw cudaMemcpy) calls this before the next cu_step_day_phase so
- * that the per-tick row copy is rebuilt.  Returns 0. */
+ * kernels, a raw cudaMemcpy) calls this before the next cu_step_day_phase or
+ * axc_step_day_phase_batch, so that the row copy those entry points keep
+ * (the per-tick copy across calls, the batch copy from one batch to the
+ * next) is laid out anew.  Returns 0. */
 int32_t axc_shard_invalidate(const ShardVramPtrs* vram);
 
 /* Capacity of the batch engine's per-tick list of deferred GSOP slots
