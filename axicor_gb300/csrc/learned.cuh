@@ -89,26 +89,29 @@ __device__ __forceinline__ uint32_t ld_bf16x2(const __nv_bfloat16* p) { return *
 // The MLP on 16 input rows by one warp (all 32 lanes): the hidden layer as 64
 // tensor-core MMAs (16 tiles of 8 units x 4 steps of 16 features, BF16 inputs
 // and weights, FP32 accumulators starting at b1), ReLU, BF16 rounding of the
-// activations, then the output layer in FP32 in a fixed order: each lane sums
-// w2[u] * h over its units (tile by tile, unit 2q before 2q + 1), then the
-// four lanes of a quad are added pairwise (xor 1, then xor 2).  a_frag holds
-// the rows' A fragments (mlp_a_frags); *yg / *yg8: the sums for rows g and
-// g + 8, the same on the four lanes of the quad, without b2 and the residual.
-__device__ __forceinline__ void mlp_warp16(const __nv_bfloat16* __restrict__ wb, const uint32_t (&a_frag)[4][4],
-                                           float* yg, float* yg8, float (*keep_a)[4] = nullptr) {
+// activations, then the output layer in FP32 in a fixed order: the units are
+// taken in 4 groups of 32 (32p .. 32p + 31); in each, a lane sums w2[u] * h
+// over its units (tile by tile, unit 2q before 2q + 1) and the four lanes of a
+// quad are added pairwise (xor 1, then xor 2); the groups are combined as
+// (G0 + G1) + (G2 + G3).  That is the order of the training kernel, whose
+// warp p holds group p, so training and inference give the same outputs.
+// *yg / *yg8: rows g and g + 8, on every lane of the quad, without b2 and the
+// residual (mlp_out).
+__device__ __forceinline__ float mlp_group_sum(const __nv_bfloat16* __restrict__ wb, const uint32_t (&a_frag)[4][4],
+                                               uint32_t grp, float* s8, float (*keep)[4] = nullptr) {
   const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
   float sg = 0.f, sg8 = 0.f;
-#pragma unroll 4
-  for (int nt = 0; nt < (int)(kHid / 8); nt++) {
-    const uint32_t u0 = 8u * nt + 2u * q;
+#pragma unroll
+  for (int nt = 0; nt < 4; nt++) {
+    const uint32_t u0 = 32u * grp + 8u * nt + 2u * q;
     const float b1a = __bfloat162float(wb[kOffB1 + u0]), b1b = __bfloat162float(wb[kOffB1 + u0 + 1]);
     float d[4] = {b1a, b1b, b1a, b1b};
-    const __nv_bfloat16* wrow = wb + (size_t)(8u * nt + g) * kFeat + 2u * q;
+    const __nv_bfloat16* wrow = wb + (size_t)(32u * grp + 8u * nt + g) * kFeat + 2u * q;
 #pragma unroll
     for (int ks = 0; ks < 4; ks++) mma_bf16_16816(d, a_frag[ks], ld_bf16x2(wrow + 16 * ks), ld_bf16x2(wrow + 16 * ks + 8));
-    if (keep_a) {
+    if (keep) {
 #pragma unroll
-      for (int e = 0; e < 4; e++) keep_a[nt][e] = d[e];
+      for (int e = 0; e < 4; e++) keep[nt][e] = d[e];
     }
     const float w2a = __bfloat162float(wb[kOffW2 + u0]), w2b = __bfloat162float(wb[kOffW2 + u0 + 1]);
     sg = __fadd_rn(sg, __fmul_rn(w2a, bf16r(fmaxf(d[0], 0.f))));
@@ -120,8 +123,17 @@ __device__ __forceinline__ void mlp_warp16(const __nv_bfloat16* __restrict__ wb,
   sg = __fadd_rn(sg, __shfl_xor_sync(kFull, sg, 2));
   sg8 = __fadd_rn(sg8, __shfl_xor_sync(kFull, sg8, 1));
   sg8 = __fadd_rn(sg8, __shfl_xor_sync(kFull, sg8, 2));
-  *yg = sg;
-  *yg8 = sg8;
+  *s8 = sg8;
+  return sg;
+}
+
+__device__ __forceinline__ void mlp_warp16(const __nv_bfloat16* __restrict__ wb, const uint32_t (&a_frag)[4][4],
+                                           float* yg, float* yg8) {
+  float p8[4], p[4];
+#pragma unroll
+  for (int grp = 0; grp < 4; grp++) p[grp] = mlp_group_sum(wb, a_frag, (uint32_t)grp, &p8[grp]);
+  *yg = __fadd_rn(__fadd_rn(p[0], p[1]), __fadd_rn(p[2], p[3]));
+  *yg8 = __fadd_rn(__fadd_rn(p8[0], p8[1]), __fadd_rn(p8[2], p8[3]));
 }
 
 // A fragments of 16 rows of FP32 features (row r at x + r * kFeat; rows >=
@@ -145,48 +157,6 @@ __device__ __forceinline__ void mlp_a_frags(const float* __restrict__ x, uint32_
 // (s + b2) + x[r][kResidF] (the residual input, BF16-rounded like the rest).
 __device__ __forceinline__ float mlp_out(const __nv_bfloat16* __restrict__ wb, float s, const float* xr) {
   return __fadd_rn(__fadd_rn(s, __bfloat162float(wb[kOffB2])), bf16r(xr[kResidF]));
-}
-
-// One hidden unit u of the MLP on the BF16-rounded input xs (shared memory):
-// returns the pre-activation (FP32, k = 0..63 in order).
-__device__ __forceinline__ float mlp_unit(const __nv_bfloat16* __restrict__ wb, uint32_t u, const float* xs) {
-  const uint4* row = reinterpret_cast<const uint4*>(wb + u * kFeat);
-  float a = __bfloat162float(wb[kOffB1 + u]);
-#pragma unroll
-  for (int c = 0; c < 8; c++) {
-    const uint4 q = __ldg(row + c);
-    const uint32_t wv[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const float lo = __uint_as_float(wv[e] << 16), hi = __uint_as_float(wv[e] & 0xFFFF0000u);
-      a = fmaf(lo, xs[c * 8 + 2 * e], a);
-      a = fmaf(hi, xs[c * 8 + 2 * e + 1], a);
-    }
-  }
-  return a;
-}
-
-// Output of the MLP for the input in xs, computed by a 128-thread block
-// (thread u = hidden unit u); a fixed reduction order, so deterministic.  The
-// network predicts a residual: its output is added to input kResidF (the
-// tile's active-synapse fraction of the tick just run), so zero weights give
-// the last-tick rule and training learns the change from tick to tick.
-__device__ __forceinline__ float mlp_block_forward(const __nv_bfloat16* __restrict__ wb, const float* xs, float* red,
-                                                   float* a_out, float* hb_out) {
-  const uint32_t u = threadIdx.x;
-  const float a = mlp_unit(wb, u, xs);
-  const float hb = bf16r(a > 0.f ? a : 0.f);
-  float part = __fmul_rn(__bfloat162float(wb[kOffW2 + u]), hb);
-  part = warp_sum_f(part);
-  __syncthreads();
-  if ((u & 31) == 0) red[u >> 5] = part;
-  __syncthreads();
-  const float y = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(red[0], red[1]), __fadd_rn(red[2], red[3])),
-                                      __bfloat162float(wb[kOffB2])),
-                            xs[kResidF]);
-  if (a_out) *a_out = a;
-  if (hb_out) *hb_out = hb;
-  return y;
 }
 
 // Block-wide exclusive scan of cnt[0..n) (1024 threads, n <= 1024 * 64) into
@@ -528,8 +498,6 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   const uint32_t u = threadIdx.x, lane = u & 31, w = u >> 5;
   __shared__ uint32_t s_cnt[8][4];
   __shared__ float s_old[kHistF];
-  __shared__ float xb[kFeat];
-  __shared__ float red[4];
   const bool seen = c.ticks_seen > 0;   // x of the previous tick is in feat[]
   // 1. the tile's neurons after the tick: 8 consecutive neurons per thread,
   //    one vector load each of timers, flags and row counts when aligned
@@ -617,21 +585,13 @@ __global__ void __launch_bounds__(128) k_learn_features(LearnDev L, ShardVramPtr
   __syncthreads();   // every read of feat[] / hist[] is done
   if (u < kHistCh * kHistLen) hist[(size_t)j * kHistF + u] = x;
   if (u == 0) hist[(size_t)j * kHistF + kHistCh * kHistLen] = (float)tot[1];
-  if (u < kFeat) {
-    xb[u] = bf16r(x);
-    feat[(size_t)j * kFeat + u] = x;
-  }
-  __syncthreads();
-  // 4. the prediction for the next tick, its capacity, the tile's partial
-  //    totals; this tick's accumulators are cleared for the next
-  const float y = mlp_block_forward(wb, xb, red, nullptr, nullptr);
+  if (u < kFeat) feat[(size_t)j * kFeat + u] = x;
+  // 4. the tile's partial totals (k_learn_predict adds the prediction for the
+  //    next tick); this tick's accumulators are cleared for the next
   if (u == 0) {
-    pred[j] = y;
-    cap[j] = tile_cap(c, y, fan[j]);
     const float err = (seen && c.policy < 0) ? fabsf(fmaxf(pred_old, 0.f) - y_now) * fj : 0.f;
     part[j] = ya;
     part[T + j] = (uint32_t)(err + 0.5f);
-    part[2 * T + j] = (uint32_t)fminf(fmaxf(y, 0.f) * fj, fj);
     part[3 * T + j] = tot[2];
     L.yacc[j] = 0;
     L.bacc[j] = 0;
@@ -730,52 +690,162 @@ __global__ void k_learn_index_done(LearnCtl* c, const ShardCtl* sc) {
   for (int q = 0; q < 9; q++) c->inrate[q] = 0.f;
 }
 
+// per tick 5b: the predictor on every tile's features, a warp per 16 tiles
+// (mlp_warp16 on the tensor cores): the next tick's predicted active-synapse
+// fraction, the tile's compaction capacity and its predicted active synapses.
+__global__ void __launch_bounds__(128) k_learn_predict(LearnDev L, const __nv_bfloat16* __restrict__ wb,
+                                                       const float* __restrict__ feat, const uint32_t* __restrict__ fan,
+                                                       float* __restrict__ pred, uint32_t* __restrict__ cap,
+                                                       uint32_t* __restrict__ part) {
+  const LearnCtl& c = *L.ctl;
+  const uint32_t T = c.T;
+  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
+  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t r0 = 16u * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); r0 < T; r0 += 16u * nw) {
+    const uint32_t nrows = min(16u, T - r0);
+    uint32_t a[4][4];
+    mlp_a_frags(feat + (size_t)r0 * kFeat, nrows, a);
+    float yg, yg8;
+    mlp_warp16(wb, a, &yg, &yg8);
+    if (q != 0) continue;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const uint32_t j = r0 + g + 8u * h;
+      if (j >= r0 + nrows) continue;
+      const float y = mlp_out(wb, h ? yg8 : yg, feat + (size_t)j * kFeat);
+      const float fj = (float)max(fan[j], 1u);
+      pred[j] = y;
+      cap[j] = tile_cap(c, y, fan[j]);
+      part[2 * T + j] = (uint32_t)fminf(fmaxf(y, 0.f) * fj, fj);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
-// MLP training: forward + backward over a slice of the minibatch per block
-// (128 threads = the hidden units), partial gradients per block, a fixed-order
-// reduction, Adam.  Loss: mean squared error over the minibatch.
+// MLP training: one block of 4 warps per 16 samples, on the tensor cores.
+// Forward: warp p computes the hidden units 32p .. 32p + 31 of the 16 samples
+// (mlp_group_sum); the output is (((G0 + G1) + (G2 + G3)) + b2) + x[kResidF],
+// as in inference.  Loss: mean squared error over the minibatch (count
+// samples, 1/count).  Backward: dy = 2 (y - t) / count; gw2[u] and gb1[u] in
+// FP32 (rows g, then g + 8, then over g by xor 4, 8, 16); dh[s][u] = dy[s] w2[u]
+// where the pre-activation is positive, rounded to BF16 for the W1 gradient
+// G1 = dh^T x, 16 units x 8 features per MMA over the 16 samples.  Each block
+// writes its partial gradient; k_mlp_reduce sums them in block order.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_mlp_grad(const __nv_bfloat16* __restrict__ wb, const float* __restrict__ X,
                                                   const float* __restrict__ Yt, const uint32_t* __restrict__ idx,
-                                                  uint32_t count, uint32_t per, float inv_count,
-                                                  float* __restrict__ partial) {
-  __shared__ float xs[kFeat];
-  __shared__ float red[4];
-  __shared__ float s_dy;
-  const uint32_t u = threadIdx.x;
-  const float w2 = __bfloat162float(wb[kOffW2 + u]);
-  float g1[kFeat];
-#pragma unroll
-  for (int k = 0; k < (int)kFeat; k++) g1[k] = 0.f;
-  float gb1 = 0.f, gw2 = 0.f, gb2 = 0.f, loss = 0.f;
-  const uint32_t s0 = blockIdx.x * per, s1 = min(count, s0 + per);
-  for (uint32_t s = s0; s < s1; s++) {
-    const uint32_t id = idx ? idx[s] : s;
-    if (u < kFeat) xs[u] = bf16r(X[(size_t)id * kFeat + u]);
-    __syncthreads();
-    float a, hb;
-    const float y = mlp_block_forward(wb, xs, red, &a, &hb);
-    if (u == 0) {
-      const float d = __fsub_rn(y, Yt[id]);
-      s_dy = __fmul_rn(__fmul_rn(2.f, d), inv_count);
-      loss = fmaf(__fmul_rn(d, d), inv_count, loss);
-    }
-    __syncthreads();
-    const float dy = s_dy;
-    gw2 = fmaf(dy, hb, gw2);
-    if (u == 0) gb2 = __fadd_rn(gb2, dy);
-    const float dh = a > 0.f ? __fmul_rn(dy, w2) : 0.f;
-    gb1 = __fadd_rn(gb1, dh);
-#pragma unroll
-    for (int k = 0; k < (int)kFeat; k++) g1[k] = fmaf(dh, xs[k], g1[k]);
-    __syncthreads();
+                                                  uint32_t count, float inv_count, float* __restrict__ partial) {
+  __shared__ __align__(16) __nv_bfloat16 xs[16][kFeat + 8];    // the samples (forward A operand)
+  __shared__ __align__(16) __nv_bfloat16 xt[kFeat][16 + 8];    // transposed (backward B operand)
+  __shared__ __align__(16) __nv_bfloat16 dht[kHid][16 + 8];    // dh transposed (backward A operand)
+  __shared__ float ysum[4][16];
+  __shared__ float s_dy[16], s_loss[16], s_x8[16];
+  const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
+  const uint32_t s0 = blockIdx.x * 16u;
+  const uint32_t ns = min(16u, count - s0);
+  for (uint32_t i = threadIdx.x; i < 16u * kFeat; i += 128u) {
+    const uint32_t r = i / kFeat, f = i % kFeat;
+    float v = 0.f;
+    if (r < ns) v = X[(size_t)(idx ? idx[s0 + r] : s0 + r) * kFeat + f];
+    const __nv_bfloat16 bv = __float2bfloat16_rn(v);
+    xs[r][f] = bv;
+    xt[f][r] = bv;
+    if (f == kResidF) s_x8[r] = __bfloat162float(bv);
   }
+  __syncthreads();
+  uint32_t a[4][4];
+#pragma unroll
+  for (int ks = 0; ks < 4; ks++) {
+    a[ks][0] = ld_bf16x2(&xs[g][16 * ks + 2 * q]);
+    a[ks][1] = ld_bf16x2(&xs[g + 8][16 * ks + 2 * q]);
+    a[ks][2] = ld_bf16x2(&xs[g][16 * ks + 8 + 2 * q]);
+    a[ks][3] = ld_bf16x2(&xs[g + 8][16 * ks + 8 + 2 * q]);
+  }
+  float acc[4][4];   // pre-activations of units 32w + 8nt + 2q (+1), rows g and g + 8
+  float sg8;
+  const float sg = mlp_group_sum(wb, a, w, &sg8, acc);
+  if (q == 0) {
+    ysum[w][g] = sg;
+    ysum[w][g + 8] = sg8;
+  }
+  __syncthreads();
+  if (threadIdx.x < 16) {
+    const uint32_t r = threadIdx.x;
+    const float y = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(ysum[0][r], ysum[1][r]), __fadd_rn(ysum[2][r], ysum[3][r])),
+                                        __bfloat162float(wb[kOffB2])),
+                              s_x8[r]);
+    float dy = 0.f, lr = 0.f;
+    if (r < ns) {
+      const float d = __fsub_rn(y, Yt[idx ? idx[s0 + r] : s0 + r]);
+      dy = __fmul_rn(__fmul_rn(2.f, d), inv_count);
+      lr = __fmul_rn(__fmul_rn(d, d), inv_count);
+    }
+    s_dy[r] = dy;
+    s_loss[r] = lr;
+  }
+  __syncthreads();
+  const float dyg = s_dy[g], dyg8 = s_dy[g + 8];
+  float gw2[4][2], gb1[4][2];
+#pragma unroll
+  for (int nt = 0; nt < 4; nt++) {
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const uint32_t u = 32u * w + 8u * nt + 2u * q + j;
+      const float w2u = __bfloat162float(wb[kOffW2 + u]);
+      const float ag = acc[nt][j], ag8 = acc[nt][2 + j];
+      gw2[nt][j] = __fadd_rn(__fmul_rn(dyg, bf16r(fmaxf(ag, 0.f))), __fmul_rn(dyg8, bf16r(fmaxf(ag8, 0.f))));
+      const float dhg = ag > 0.f ? __fmul_rn(dyg, w2u) : 0.f, dhg8 = ag8 > 0.f ? __fmul_rn(dyg8, w2u) : 0.f;
+      gb1[nt][j] = __fadd_rn(dhg, dhg8);
+      dht[u][g] = __float2bfloat16_rn(dhg);
+      dht[u][g + 8] = __float2bfloat16_rn(dhg8);
+    }
+  }
+#pragma unroll
+  for (int nt = 0; nt < 4; nt++) {
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+#pragma unroll
+      for (int o = 4; o < 32; o <<= 1) {
+        gw2[nt][j] = __fadd_rn(gw2[nt][j], __shfl_xor_sync(kFull, gw2[nt][j], o));
+        gb1[nt][j] = __fadd_rn(gb1[nt][j], __shfl_xor_sync(kFull, gb1[nt][j], o));
+      }
+    }
+  }
+  __syncthreads();
   float* Pp = partial + (size_t)blockIdx.x * (kParams + 1);
 #pragma unroll
-  for (int k = 0; k < (int)kFeat; k++) Pp[u * kFeat + k] = g1[k];
-  Pp[kOffB1 + u] = gb1;
-  Pp[kOffW2 + u] = gw2;
-  if (u == 0) {
+  for (int mt = 0; mt < 2; mt++) {
+    const uint32_t ub = 32u * w + 16u * mt;
+    const uint32_t am[4] = {ld_bf16x2(&dht[ub + g][2 * q]), ld_bf16x2(&dht[ub + g + 8][2 * q]),
+                            ld_bf16x2(&dht[ub + g][8 + 2 * q]), ld_bf16x2(&dht[ub + g + 8][8 + 2 * q])};
+#pragma unroll
+    for (int nf = 0; nf < 8; nf++) {
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+      mma_bf16_16816(d, am, ld_bf16x2(&xt[8 * nf + g][2 * q]), ld_bf16x2(&xt[8 * nf + g][8 + 2 * q]));
+      const uint32_t f = 8u * nf + 2u * q;
+      Pp[(size_t)(ub + g) * kFeat + f] = d[0];
+      Pp[(size_t)(ub + g) * kFeat + f + 1] = d[1];
+      Pp[(size_t)(ub + g + 8) * kFeat + f] = d[2];
+      Pp[(size_t)(ub + g + 8) * kFeat + f + 1] = d[3];
+    }
+  }
+  if (g == 0) {
+#pragma unroll
+    for (int nt = 0; nt < 4; nt++) {
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const uint32_t u = 32u * w + 8u * nt + 2u * q + j;
+        Pp[kOffB1 + u] = gb1[nt][j];
+        Pp[kOffW2 + u] = gw2[nt][j];
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    float gb2 = 0.f, loss = 0.f;
+    for (int r = 0; r < 16; r++) {
+      gb2 = __fadd_rn(gb2, s_dy[r]);
+      loss = __fadd_rn(loss, s_loss[r]);
+    }
     Pp[kOffB2] = gb2;
     Pp[kParams] = loss;
   }
@@ -812,17 +882,21 @@ __global__ void __launch_bounds__(256) k_mlp_adam(float* __restrict__ master, fl
   wb[p] = __float2bfloat16_rn(w);
 }
 
+// Predictions for `count` rows of X (axc_mlp_predict), a warp per 16 rows.
 __global__ void __launch_bounds__(128) k_mlp_predict(const __nv_bfloat16* __restrict__ wb,
                                                      const float* __restrict__ X, uint32_t count,
                                                      float* __restrict__ out) {
-  __shared__ float xs[kFeat];
-  __shared__ float red[4];
-  for (uint32_t s = blockIdx.x; s < count; s += gridDim.x) {
-    if (threadIdx.x < kFeat) xs[threadIdx.x] = bf16r(X[(size_t)s * kFeat + threadIdx.x]);
-    __syncthreads();
-    const float y = mlp_block_forward(wb, xs, red, nullptr, nullptr);
-    if (threadIdx.x == 0) out[s] = y;
-    __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
+  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t r0 = 16u * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); r0 < count; r0 += 16u * nw) {
+    const uint32_t nrows = min(16u, count - r0);
+    uint32_t a[4][4];
+    mlp_a_frags(X + (size_t)r0 * kFeat, nrows, a);
+    float yg, yg8;
+    mlp_warp16(wb, a, &yg, &yg8);
+    if (q != 0) continue;
+    if (g < nrows) out[r0 + g] = mlp_out(wb, yg, X + (size_t)(r0 + g) * kFeat);
+    if (g + 8u < nrows) out[r0 + g + 8] = mlp_out(wb, yg8, X + (size_t)(r0 + g + 8) * kFeat);
   }
 }
 
@@ -1061,6 +1135,8 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool la
     k_learn_features<<<L.T, 128, 0, st>>>(D, L.v, N, r.cnt, L.fan, L.axn, L.hist, L.feat, L.pred, L.cap, L.part,
                                           L.wb, L.X, L.Y, L.nv ? L.stage + (size_t)(k + 1) * L.words : nullptr,
                                           L.words, L.nv, s.ctl);
+  if (features_on && L.T)
+    k_learn_predict<<<(L.T + 63) / 64, 128, 0, st>>>(D, L.wb, L.feat, L.fan, L.pred, L.cap, L.part);
   return cudaGetLastError();
 }
 
@@ -1431,7 +1507,7 @@ int32_t axc_learned_train(void* handle, uint32_t epochs, uint32_t batch, float l
     for (uint32_t b0 = 0; b0 < ntr && e == cudaSuccess; b0 += batch) {
       const uint32_t cnt = std::min(batch, ntr - b0);
       const uint32_t nb = (cnt + kGradPer - 1) / kGradPer;
-      k_mlp_grad<<<nb, 128, 0, st>>>(L->wb, L->X, L->Y, L->idx + b0, cnt, kGradPer, 1.f / (float)cnt, L->partial);
+      k_mlp_grad<<<nb, 128, 0, st>>>(L->wb, L->X, L->Y, L->idx + b0, cnt, 1.f / (float)cnt, L->partial);
       k_mlp_reduce<<<(kParams + 1 + 255) / 256, 256, 0, st>>>(L->partial, nb, L->grad);
       L->adam_step++;
       const float c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)L->adam_step)));
@@ -1450,7 +1526,7 @@ int32_t axc_learned_train(void* handle, uint32_t epochs, uint32_t batch, float l
     *out_val = 0.f;
     if (nval) {
       const uint32_t nb = (nval + kGradPer - 1) / kGradPer;
-      k_mlp_grad<<<nb, 128, 0, st>>>(L->wb, L->X + (size_t)ntr * kFeat, L->Y + ntr, nullptr, nval, kGradPer,
+      k_mlp_grad<<<nb, 128, 0, st>>>(L->wb, L->X + (size_t)ntr * kFeat, L->Y + ntr, nullptr, nval,
                                      1.f / (float)nval, L->partial);
       k_mlp_reduce<<<(kParams + 1 + 255) / 256, 256, 0, st>>>(L->partial, nb, L->grad);
       e = cudaMemcpyAsync(out_val, L->grad + kParams, 4, cudaMemcpyDeviceToHost, st);
@@ -1485,7 +1561,7 @@ int32_t axc_mlp_loss_grad(const float* d_params, const float* d_x, const float* 
   if (e == cudaSuccess) e = cudaMalloc(&grad, ((size_t)kParams + 1) * 4);
   if (e == cudaSuccess) {
     k_mlp_to_bf16<<<(kParams + 255) / 256, 256, 0, st>>>(d_params, wb);
-    k_mlp_grad<<<nb, 128, 0, st>>>(wb, d_x, d_y, nullptr, count, kGradPer, 1.f / (float)count, partial);
+    k_mlp_grad<<<nb, 128, 0, st>>>(wb, d_x, d_y, nullptr, count, 1.f / (float)count, partial);
     k_mlp_reduce<<<(kParams + 1 + 255) / 256, 256, 0, st>>>(partial, nb, grad);
     e = cudaMemcpyAsync(d_grad, grad, (size_t)kParams * 4, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess && d_loss) e = cudaMemcpyAsync(d_loss, grad + kParams, 4, cudaMemcpyDeviceToDevice, st);
@@ -1505,7 +1581,7 @@ int32_t axc_mlp_predict(const float* d_params, const float* d_x, uint32_t count,
   cudaError_t e = cudaMalloc(&wb, (size_t)kParams * 2);
   if (e == cudaSuccess) {
     k_mlp_to_bf16<<<(kParams + 255) / 256, 256, 0, st>>>(d_params, wb);
-    k_mlp_predict<<<std::min(count, 4096u), 128, 0, st>>>(wb, d_x, count, d_out);
+    k_mlp_predict<<<std::min((count + 63u) / 64u, 4096u), 128, 0, st>>>(wb, d_x, count, d_out);
     e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
   }

@@ -2,23 +2,29 @@
 imported by tests and never by the engine).
 
 The reference has no learned predictor; this restates the engine's own
-arithmetic so that the GPU forward, loss and gradients can be checked
-value for value:
+arithmetic so that the GPU forward, loss and gradients can be checked:
 
 - parameters and inputs are rounded to BF16 (round to nearest even);
-- hidden unit u: a = b1[u], then a = fma(W1[u][k], x[k], a) for k = 0..63;
-  hb = bf16(relu(a)); part = w2[u] * hb (exact in FP32);
-- output: a butterfly sum over each warp of 32 units (xor 16, 8, 4, 2, 1),
-  then (w0 + w1) + (w2 + w3), then + b2, then + x[RESID] (the network
-  predicts the change from the last tick's active-synapse fraction);
-- loss = mean (y - t)^2 accumulated as fma(d * d, 1/B, loss); dy = (2 d)(1/B);
-  per block of 16 samples, in sample order: gw2 = fma(dy, hb, gw2),
-  gb2 += dy, dh = dy * w2 if a > 0 else 0, gb1 += dh, g1[k] = fma(dh, x[k], g1[k]);
-  block partials are summed in block order.
+- hidden pre-activations a = b1 + W1 x: the kernels accumulate the exact
+  products of BF16 values in FP32 on the tensor cores (mma m16n8k16), whose
+  internal order is not specified; here they are summed in float64 and
+  rounded once to float32, so a can differ from the GPU's in its last bits
+  (and, rarely, the BF16 rounding of the activation with it);
+- hb = bf16(relu(a)); the output layer in the kernels' fixed FP32 order: the
+  units in 4 groups of 32 (32p .. 32p + 31); in a group, lane q (0..3) sums
+  w2[u] * hb[u] over the tiles nt = 0..3 for u = 32p + 8nt + 2q, then +1;
+  lanes (q0 + q1) + (q2 + q3); groups (G0 + G1) + (G2 + G3); + b2;
+  + x[RESID] (the network predicts the change from the last tick's
+  active-synapse fraction);
+- per block of 16 samples: dy = (2 d) / B; loss term d^2 / B; gw2[u] and
+  gb1[u] from the two rows of each lane (g, g + 8) reduced over g = 0..7 in a
+  butterfly (xor 1, 2, 4 of g); dh = dy w2 where a > 0, rounded to BF16 for
+  the W1 gradient (dh^T x on the tensor cores: float64 here, then float32);
+  gb2 and the loss summed over the 16 rows in order; block partials summed in
+  block order.
 
-FMA is emulated as one float64 operation rounded to float32 (the product of
-two float32 values is exact in float64); `grad_float64` is the plain float64
-gradient used to pin the backward pass by finite differences.
+`loss_float64` / `grad_float64` are the plain float64 loss and gradient,
+used to pin the backward pass by finite differences.
 """
 from __future__ import annotations
 
@@ -50,58 +56,81 @@ def unpack(params: np.ndarray):
     return (p[:OFF_B1].reshape(HIDDEN, FEATURES), p[OFF_B1:OFF_W2], p[OFF_W2:OFF_B2], p[OFF_B2])
 
 
-def forward(params: np.ndarray, x: np.ndarray):
-    """Returns (y[B], a[B][128], hb[B][128]) exactly as the kernels compute them."""
+def _hidden(params: np.ndarray, x: np.ndarray):
     W1, b1, w2, b2 = unpack(params)
     xb = bf16(x)
-    a = np.broadcast_to(b1, (xb.shape[0], HIDDEN)).astype(np.float32).copy()
-    for k in range(FEATURES):
-        a = fma(W1[:, k][None, :], xb[:, k][:, None], a)
+    a = (b1[None, :].astype(np.float64) + xb.astype(np.float64) @ W1.T.astype(np.float64)).astype(np.float32)
     hb = bf16(np.maximum(a, f32(0)))
-    part = (w2[None, :].astype(np.float32) * hb).astype(np.float32)
-    v = part.reshape(-1, 4, 32).copy()
-    lanes = np.arange(32)
-    for o in (16, 8, 4, 2, 1):
-        v = (v + v[:, :, lanes ^ o]).astype(np.float32)
-    r = v[:, :, 0]
-    y = ((r[:, 0] + r[:, 1]).astype(np.float32) + (r[:, 2] + r[:, 3]).astype(np.float32)).astype(np.float32)
+    return W1, b1, w2, b2, xb, a, hb
+
+
+def _output(w2, b2, xb, hb):
+    part = (w2[None, :].astype(np.float32) * hb).astype(np.float32)   # exact: BF16 x BF16
+    groups = []
+    for grp in range(4):
+        lanes = []
+        for q in range(4):
+            acc = np.zeros(hb.shape[0], np.float32)
+            for nt in range(4):
+                u0 = 32 * grp + 8 * nt + 2 * q
+                acc = (acc + part[:, u0]).astype(np.float32)
+                acc = (acc + part[:, u0 + 1]).astype(np.float32)
+            lanes.append(acc)
+        groups.append(((lanes[0] + lanes[1]).astype(np.float32) + (lanes[2] + lanes[3]).astype(np.float32))
+                      .astype(np.float32))
+    y = ((groups[0] + groups[1]).astype(np.float32) + (groups[2] + groups[3]).astype(np.float32)).astype(np.float32)
     y = (y + f32(b2)).astype(np.float32)
-    y = (y + xb[:, RESID]).astype(np.float32)
-    return y, a, hb
+    return (y + xb[:, RESID]).astype(np.float32)
+
+
+def forward(params: np.ndarray, x: np.ndarray):
+    """Returns (y[B], a[B][128], hb[B][128]) as the kernels compute them (a up to its last bits)."""
+    W1, b1, w2, b2, xb, a, hb = _hidden(params, x)
+    return _output(w2, b2, xb, hb), a, hb
+
+
+def _butterfly8(v):
+    """Sum over axis 0 (8 entries, g = 0..7) as xor 1, 2, 4 shuffles add them."""
+    v = v.astype(np.float32)
+    for o in (1, 2, 4):
+        v = (v + v[np.arange(8) ^ o]).astype(np.float32)
+    return v[0]
 
 
 def loss_grad(params: np.ndarray, x: np.ndarray, t: np.ndarray):
     """Mean squared error and its gradient with the kernels' order of operations."""
-    W1, b1, w2, b2 = unpack(params)
-    xb = bf16(x)
-    y, a, hb = forward(params, x)
+    W1, b1, w2, b2, xb, a, hb = _hidden(params, x)
+    y = _output(w2, b2, xb, hb)
     B = x.shape[0]
     ic = f32(1.0) / f32(B)
     nb = (B + GRAD_PER - 1) // GRAD_PER
-    partial = np.zeros((nb, PARAMS + 1), np.float32)
-    for blk in range(nb):
-        g1 = np.zeros((HIDDEN, FEATURES), np.float32)
-        gb1 = np.zeros(HIDDEN, np.float32)
-        gw2 = np.zeros(HIDDEN, np.float32)
-        gb2 = f32(0)
-        loss = f32(0)
-        for s in range(blk * GRAD_PER, min(B, (blk + 1) * GRAD_PER)):
-            d = f32(y[s] - f32(t[s]))
-            dy = f32(f32(f32(2.0) * d) * ic)
-            loss = fma(f32(d * d), ic, loss)
-            gw2 = fma(dy, hb[s], gw2)
-            gb2 = f32(gb2 + dy)
-            dh = np.where(a[s] > 0, (dy * w2).astype(np.float32), f32(0)).astype(np.float32)
-            gb1 = (gb1 + dh).astype(np.float32)
-            g1 = fma(dh[:, None], xb[s][None, :], g1)
-        partial[blk, :OFF_B1] = g1.reshape(-1)
-        partial[blk, OFF_B1:OFF_W2] = gb1
-        partial[blk, OFF_W2:OFF_B2] = gw2
-        partial[blk, OFF_B2] = gb2
-        partial[blk, PARAMS] = loss
     tot = np.zeros(PARAMS + 1, np.float32)
     for blk in range(nb):
-        tot = (tot + partial[blk]).astype(np.float32)
+        rows = np.arange(blk * GRAD_PER, (blk + 1) * GRAD_PER)
+        valid = rows < B
+        r = np.where(valid, rows, 0)
+        d = np.where(valid, (y[r] - np.asarray(t, np.float32)[r]).astype(np.float32), f32(0)).astype(np.float32)
+        dy = ((f32(2.0) * d).astype(np.float32) * ic).astype(np.float32)
+        lt = ((d * d).astype(np.float32) * ic).astype(np.float32)
+        ab = np.where(valid[:, None], a[r], f32(0)).astype(np.float32)
+        hbb = np.where(valid[:, None], hb[r], f32(0)).astype(np.float32)
+        xbb = np.where(valid[:, None], xb[r], f32(0)).astype(np.float32)
+        dh = np.where(ab > 0, (dy[:, None] * w2[None, :]).astype(np.float32), f32(0)).astype(np.float32)
+        # rows g and g + 8 of each lane, then the butterfly over g
+        v_w2 = ((dy[:8, None] * hbb[:8]).astype(np.float32) + (dy[8:, None] * hbb[8:]).astype(np.float32))
+        v_b1 = (dh[:8] + dh[8:]).astype(np.float32)
+        part = np.zeros(PARAMS + 1, np.float32)
+        part[:OFF_B1] = (bf16(dh).astype(np.float64).T @ xbb.astype(np.float64)).astype(np.float32).reshape(-1)
+        part[OFF_B1:OFF_W2] = _butterfly8(v_b1)
+        part[OFF_W2:OFF_B2] = _butterfly8(v_w2)
+        gb2 = f32(0)
+        loss = f32(0)
+        for k in range(GRAD_PER):
+            gb2 = f32(gb2 + dy[k])
+            loss = f32(loss + lt[k])
+        part[OFF_B2] = gb2
+        part[PARAMS] = loss
+        tot = (tot + part).astype(np.float32)
     return float(tot[PARAMS]), tot[:PARAMS]
 
 

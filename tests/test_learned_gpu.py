@@ -18,25 +18,30 @@ pytestmark = pytest.mark.gpu
 
 
 def test_mlp_gradient_matches_oracle(gpu):
+    """The tensor-core training kernel against the oracle's restatement of its order.  The tolerance is the
+    tensor cores' FP32 accumulation of the hidden layer (unspecified order: last bits of a, and through them,
+    rarely, one BF16 step of an activation): loss within 1e-5, every gradient entry within 2e-3 of the largest,
+    and the whole gradient within 1e-3 in relative L2 norm."""
     rng = np.random.Generator(np.random.PCG64(11))
     p = M.init_params(7)
     x = rng.uniform(0, 1, (200, M.FEATURES)).astype(np.float32)
     t = rng.uniform(0, 1, 200).astype(np.float32)
     loss, g = L.mlp_loss_grad(p, x, t)
     lo, go = M.loss_grad(p, x, t)
-    assert loss == pytest.approx(lo, rel=1e-6)
-    assert np.mean(g == go) > 0.99                      # value for value but for rare FMA double rounding
-    assert np.abs(g - go).max() <= 1e-5 * np.abs(go).max()
+    assert loss == pytest.approx(lo, rel=1e-5)
+    assert np.abs(g - go).max() <= 2e-3 * np.abs(go).max()
+    assert np.linalg.norm(g - go) <= 1e-3 * np.linalg.norm(go)
 
 
 def test_mlp_predict_matches_oracle(gpu):
+    """Predictions on the tensor cores against the oracle's restatement, within the same tolerance."""
     rng = np.random.Generator(np.random.PCG64(12))
     p = M.init_params(8)
     x = rng.uniform(0, 1, (300, M.FEATURES)).astype(np.float32)
     y = L.mlp_predict(p, x)
     yo, _, _ = M.forward(p, x)
-    assert np.mean(y == yo) > 0.99
-    assert np.abs(y - yo).max() <= 1e-5 * max(1.0, np.abs(yo).max())
+    assert np.mean(y == yo) > 0.9
+    assert np.abs(y - yo).max() <= 1e-3 * max(1.0, np.abs(yo).max())
 
 
 class LBrain:
