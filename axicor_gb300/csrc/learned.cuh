@@ -690,34 +690,53 @@ __global__ void k_learn_index_done(LearnCtl* c, const ShardCtl* sc) {
   for (int q = 0; q < 9; q++) c->inrate[q] = 0.f;
 }
 
-// per tick 5b: the predictor on every tile's features, a warp per 16 tiles
-// (mlp_warp16 on the tensor cores): the next tick's predicted active-synapse
-// fraction, the tile's compaction capacity and its predicted active synapses.
+// The output of the MLP for 16 rows of x by a block of 4 warps: warp p computes
+// the sums of unit group p (mlp_group_sum) and the first 16 threads combine
+// them in mlp_warp16's order, so the result equals mlp_warp16's; *y_out (row
+// threadIdx.x, for threads < nrows) gets (s + b2) + x[kResidF].  All 128
+// threads must call it.
+__device__ __forceinline__ bool mlp_block16(const __nv_bfloat16* __restrict__ wb, const float* __restrict__ x,
+                                            uint32_t nrows, float* y_out) {
+  __shared__ float s_grp[4][16];
+  const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
+  uint32_t a[4][4];
+  mlp_a_frags(x, nrows, a);
+  float s8;
+  const float s0 = mlp_group_sum(wb, a, w, &s8);
+  if (q == 0) {
+    s_grp[w][g] = s0;
+    s_grp[w][g + 8] = s8;
+  }
+  __syncthreads();
+  const uint32_t r = threadIdx.x;
+  bool ok = false;
+  if (r < nrows) {
+    const float s = __fadd_rn(__fadd_rn(s_grp[0][r], s_grp[1][r]), __fadd_rn(s_grp[2][r], s_grp[3][r]));
+    *y_out = mlp_out(wb, s, x + (size_t)r * kFeat);
+    ok = true;
+  }
+  __syncthreads();   // s_grp is free for the next call
+  return ok;
+}
+
+// per tick 5b: the predictor on every tile's features, a block of 4 warps
+// per 16 tiles on the tensor cores (mlp_block16): the next tick's predicted
+// active-synapse fraction, the tile's compaction capacity and its predicted
+// active synapses.
 __global__ void __launch_bounds__(128) k_learn_predict(LearnDev L, const __nv_bfloat16* __restrict__ wb,
                                                        const float* __restrict__ feat, const uint32_t* __restrict__ fan,
                                                        float* __restrict__ pred, uint32_t* __restrict__ cap,
                                                        uint32_t* __restrict__ part) {
   const LearnCtl& c = *L.ctl;
   const uint32_t T = c.T;
-  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
-  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t r0 = 16u * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); r0 < T; r0 += 16u * nw) {
-    const uint32_t nrows = min(16u, T - r0);
-    uint32_t a[4][4];
-    mlp_a_frags(feat + (size_t)r0 * kFeat, nrows, a);
-    float yg, yg8;
-    mlp_warp16(wb, a, &yg, &yg8);
-    if (q != 0) continue;
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const uint32_t j = r0 + g + 8u * h;
-      if (j >= r0 + nrows) continue;
-      const float y = mlp_out(wb, h ? yg8 : yg, feat + (size_t)j * kFeat);
-      const float fj = (float)max(fan[j], 1u);
-      pred[j] = y;
-      cap[j] = tile_cap(c, y, fan[j]);
-      part[2 * T + j] = (uint32_t)fminf(fmaxf(y, 0.f) * fj, fj);
-    }
+  for (uint32_t r0 = 16u * blockIdx.x; r0 < T; r0 += 16u * gridDim.x) {
+    float y;
+    if (!mlp_block16(wb, feat + (size_t)r0 * kFeat, min(16u, T - r0), &y)) continue;
+    const uint32_t j = r0 + threadIdx.x;
+    const float fj = (float)max(fan[j], 1u);
+    pred[j] = y;
+    cap[j] = tile_cap(c, y, fan[j]);
+    part[2 * T + j] = (uint32_t)fminf(fmaxf(y, 0.f) * fj, fj);
   }
 }
 
@@ -882,21 +901,14 @@ __global__ void __launch_bounds__(256) k_mlp_adam(float* __restrict__ master, fl
   wb[p] = __float2bfloat16_rn(w);
 }
 
-// Predictions for `count` rows of X (axc_mlp_predict), a warp per 16 rows.
+// Predictions for `count` rows of X (axc_mlp_predict), a block of 4 warps
+// per 16 rows.
 __global__ void __launch_bounds__(128) k_mlp_predict(const __nv_bfloat16* __restrict__ wb,
                                                      const float* __restrict__ X, uint32_t count,
                                                      float* __restrict__ out) {
-  const uint32_t lane = threadIdx.x & 31u, g = lane >> 2, q = lane & 3u;
-  const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t r0 = 16u * (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); r0 < count; r0 += 16u * nw) {
-    const uint32_t nrows = min(16u, count - r0);
-    uint32_t a[4][4];
-    mlp_a_frags(X + (size_t)r0 * kFeat, nrows, a);
-    float yg, yg8;
-    mlp_warp16(wb, a, &yg, &yg8);
-    if (q != 0) continue;
-    if (g < nrows) out[r0 + g] = mlp_out(wb, yg, X + (size_t)(r0 + g) * kFeat);
-    if (g + 8u < nrows) out[r0 + g + 8] = mlp_out(wb, yg8, X + (size_t)(r0 + g + 8) * kFeat);
+  for (uint32_t r0 = 16u * blockIdx.x; r0 < count; r0 += 16u * gridDim.x) {
+    float y;
+    if (mlp_block16(wb, X + (size_t)r0 * kFeat, min(16u, count - r0), &y)) out[r0 + threadIdx.x] = y;
   }
 }
 
@@ -1136,7 +1148,7 @@ static cudaError_t learned_tick(Learned& L, ShardScratch& s, uint32_t k, bool la
                                           L.wb, L.X, L.Y, L.nv ? L.stage + (size_t)(k + 1) * L.words : nullptr,
                                           L.words, L.nv, s.ctl);
   if (features_on && L.T)
-    k_learn_predict<<<(L.T + 63) / 64, 128, 0, st>>>(D, L.wb, L.feat, L.fan, L.pred, L.cap, L.part);
+    k_learn_predict<<<(L.T + 15) / 16, 128, 0, st>>>(D, L.wb, L.feat, L.fan, L.pred, L.cap, L.part);
   return cudaGetLastError();
 }
 
@@ -1581,7 +1593,7 @@ int32_t axc_mlp_predict(const float* d_params, const float* d_x, uint32_t count,
   cudaError_t e = cudaMalloc(&wb, (size_t)kParams * 2);
   if (e == cudaSuccess) {
     k_mlp_to_bf16<<<(kParams + 255) / 256, 256, 0, st>>>(d_params, wb);
-    k_mlp_predict<<<std::min((count + 63u) / 64u, 4096u), 128, 0, st>>>(wb, d_x, count, d_out);
+    k_mlp_predict<<<std::min((count + 15u) / 16u, 8192u), 128, 0, st>>>(wb, d_x, count, d_out);
     e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaGetLastError();
   }

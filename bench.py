@@ -143,8 +143,8 @@ class Clocks:
 
 
 # DRAM traffic per launch of the dominant kernel (ncu dram__bytes_read.sum + dram__bytes_write.sum) from one
-# capture of the same kernel on the same workload in its steady state
-TRAFFIC = {("plain-1.5M", "k_rows_update"): 337.3e6}
+# capture of the same kernel on the same workload in its steady state (tick ~1,200)
+TRAFFIC = {("plain-1.5M", "k_rows_update_lsum"): 66.5e6, ("plain-1.5M", "k_rows_prologue_plain"): 66.1e6}
 
 
 def cpu_model() -> str | None:
