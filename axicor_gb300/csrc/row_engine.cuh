@@ -2075,7 +2075,9 @@ static void launch_rows_gsop(const ShardVramPtrs& v, ShardScratch& s, uint32_t A
 // prologue; a per-tick call (cu_step_day_phase) passes them to the prologue,
 // applies its pushes before it returns, and writes GSOP's weight changes
 // through to the columnar blob (its row cache outlives the call).  ev
-// (optional) gets the stage boundaries 2..5 recorded (GSOP is part of update).
+// (optional) gets the stage boundaries 2..5 recorded: after the prologue,
+// after the 8-lane pass, after the lit-sum pass, after fix-up and push (GSOP
+// is part of the update passes).
 cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const TickArgs& a, cudaStream_t stream,
                              cudaEvent_t* ev, bool have_incoming) {
   RowCache& r = *s.rows;
@@ -2100,17 +2102,19 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
     wt.cnt = r.cnt;
     wt.N = N;
   }
-  // stages: ev[2]..ev[3] the update pass with GSOP, ev[3]..ev[4] fix-up and push.
-  // Both forms are launched; each returns at once on the other's ticks.
+  // stages: ev[2]..ev[3] the 8-lane pass, ev[3]..ev[4] the lit-sum pass (both
+  // with GSOP; both are launched and each returns at once on the other's
+  // ticks), ev[4]..ev[5] fix-up and push.
   const uint32_t fix_cap = min(a.fix_cap, kFixCap);
   launch_rows_update<true>(v, s, N, A, a.k, fix_cap, nullptr, stream, wt);
+  if (ev) cudaEventRecord(ev[3], stream);
   if (per_tick)
     k_rows_update_lsum<true><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                           s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt, nullptr);
   else
     k_rows_update_lsum<false><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
                                                            s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt, nullptr);
-  if (ev) cudaEventRecord(ev[3], stream);
+  if (ev) cudaEventRecord(ev[4], stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
   k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
                                             a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0, wt);
@@ -2118,10 +2122,7 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   if (!a.defer_push)
     k_rows_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, r.eval, v.soma_flags, N,
                                              nullptr, nullptr, 0, s.ctl, a.k);
-  if (ev) {
-    cudaEventRecord(ev[4], stream);
-    cudaEventRecord(ev[5], stream);
-  }
+  if (ev) cudaEventRecord(ev[5], stream);
   return cudaGetLastError();
 }
 

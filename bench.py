@@ -311,19 +311,21 @@ def run_gb300(args, dist: Dist) -> dict | None:
         raise RuntimeError(f"axc_profile_ticks failed: {err}")
     stage_ms = list(out_ms)
     if engine == 1:
-        names = ["network_ids", "prologue", "update", "gsop_fixup_push", "unused"]
-        kernels = {"prologue": "k_rows_prologue_plain", "update": "k_rows_update",
+        names = ["network_ids", "prologue", "update", "update_lsum", "gsop_fixup_push"]
+        kernels = {"prologue": "k_rows_prologue_plain", "update": "k_rows_update", "update_lsum": "k_rows_update_lsum",
                    "gsop_fixup_push": "k_rows_fixup+k_rows_push"}
     else:
         names = ["network_ids", "axons", "update", "push", "gsop"]
         kernels = {"axons": "k_axons", "update": "k_update", "push": "k_push", "gsop": "k_gsop"}
     top = int(np.argmax(stage_ms))
     ev, hits, spk, gs, nev, lit_ticks, tested = (int(x) for x in out_cnt)
-    if engine == 1 and lit_ticks:
-        kernels["update"] = "k_rows_update_lsum" if lit_ticks == prof_ticks else "k_rows_update+k_rows_update_lsum"
     A_ = lay.total_axons
-    if engine == 1 and names[top] == "update":
-        kb = rows_update_kernel_bytes(ev, nev, spk, prof_ticks, lit_ticks, tested)
+    if engine == 1 and names[top] in ("update", "update_lsum"):
+        # the bytes of the ticks that pass ran (the other returns at once)
+        f = lit_ticks / prof_ticks
+        both = rows_update_kernel_bytes(ev, nev, spk, prof_ticks, lit_ticks, tested)
+        full_only = (1 - f) * (6 * ev + 24 * nev + 4 * spk)
+        kb = full_only if names[top] == "update" else both - full_only
     elif names[top] == "update":
         kb = update_kernel_bytes(prof_ticks, ev, spk, lay.padded_n)
     elif names[top] == "gsop":

@@ -343,8 +343,9 @@ void axc_io_pipeline_destroy(void* handle);
  * per-tick kernels of cu_step_day_phase; engine 1: the batch engine's
  * neuron-major kernels (the ticks then form one batch, rows built before and
  * weights written back after).  Sets out_ms[5] to the stage times in
- * milliseconds (network ids, axons, update, push, GSOP; with engine 1 GSOP is
- * part of update and "push" includes the GSOP fix-up) and out_counts[7] to
+ * milliseconds: engine 0 network ids, axons, update, push, GSOP; engine 1
+ * network ids, prologue, the 8-lane pass, the lit-sum pass (both with GSOP;
+ * each returns at once on the other's ticks), fix-up and push; and out_counts[7] to
  * the ticks' totals of evaluated slots, hits, spikes, GSOP slots, evaluated
  * (non-refractory) neurons, ticks on the lit-sum form and the slots that form
  * tested (the counters [1]..[7] of axc_shard_counters).  Synchronous. */
