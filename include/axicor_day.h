@@ -247,11 +247,12 @@ int32_t axc_last_spikes(const ShardVramPtrs* vram, uint32_t* out_count, uint32_t
  * once into a CUDA graph per (shard, batch shape) and replayed.  The
  * neuron-major row copy the ticks run on is kept from one batch to the next
  * (its weights are written back to the .state blob at the end of every
- * batch) and laid out anew at the second batch, then after 100, 200, 400,
- * ... up to every 1,600 ticks, and whenever the shard's memory or the LUT
- * may have changed (followed again by one at the next batch): after any
- * entry point of this library that writes them, per-tick calls, and
- * axc_shard_invalidate.
+ * batch).  The device decides before each batch whether to lay it out anew:
+ * at every batch while the layout leaves more than an eighth of the live
+ * slots outside its lit-sum groups (the weights are still freezing), then
+ * after 100, 200, 400, ... up to every 1,600 ticks; and for sure after the
+ * shard's memory or the LUT may have changed: after any entry point of this
+ * library that writes them, per-tick calls, and axc_shard_invalidate.
  * h_output_history, when not NULL, receives num_outputs x batch bytes
  * (device to host on the stream).  h_spike_counts may be NULL (no network
  * spikes).  Asynchronous on `stream` unless h_output_history is given, in

@@ -1,8 +1,9 @@
 """The batch path keeps its neuron-major row copy from one batch to the next.
 
-axc_step_day_phase_batch lays the rows out at the first two batches and again
-after 100, 200, 400, ... ticks (up to 1,600), and in between starts each batch
-on the last batch's rows (written back to the .state blob at every batch end).
+axc_step_day_phase_batch keeps its rows from one batch to the next (written
+back to the .state blob at every batch end); the device lays them out anew at
+every batch while the layout misses the lit-sum criterion, then after 100,
+200, 400, ... ticks (up to 1,600).
 The copy must be laid out anew whenever the shard's memory or the LUT changed
 between batches by any route the reference uses (shard_thread.rs:295-350:
 sort-and-prune, the sprouting upload through gpu_memcpy_host_to_device;
@@ -85,8 +86,8 @@ def _raw_htod(dev_ptr, host):
 
 
 def test_batches_on_kept_rows_through_relayouts(gpu):
-    """40 batches of 20 ticks with nothing in between: the rows are laid out at ticks 0, 20, 120, 320 and
-    720 and reused by every other batch, with GSOP still moving weights (several movable inertia ranks)."""
+    """40 batches of 20 ticks with nothing in between, with GSOP still moving weights (several movable
+    inertia ranks): layouts and kept copies alternate as the device decides, every batch bit-exact."""
     w = W.small(dims=(16, 16, 8), slots=80, inputs=64, p=0.1)
     for v in (0, 1):
         w.lut[v]["inertia_curve"] = np.array([128, 110, 90, 70, 50] + [0] * 11, np.uint8)
