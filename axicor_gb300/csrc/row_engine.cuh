@@ -42,6 +42,36 @@ namespace {
 
 constexpr uint32_t kRowStride = AXC_MAX_DENDRITES;   // slots per neuron row
 constexpr uint32_t kInf = 0xFFFFFFFFu;
+
+// Programmatic dependent launch inside a tick's kernel chain (prologue ->
+// 8-lane pass -> lit-sum pass -> fix-up -> push).  A kernel
+// launched with launch_chain(pdl = true) may be scheduled while the kernel
+// before it on the stream still runs; its first statement is chain_wait(),
+// which returns once that kernel has completed and its writes are visible, so
+// only the launch and the block scheduling overlap.  Every block passes
+// chain_wait() before it can exit, so a kernel's completion implies its
+// predecessor's, and the chain stays ordered end to end.  chain_open() then
+// lets the next kernel of the chain be scheduled (after this grid's last block
+// started and passed its own wait).  Both are no-ops for a kernel launched
+// without the attribute.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_open() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... P, typename... Args>
+static void launch_chain(void (*kern)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream, bool pdl,
+                         Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 constexpr uint32_t kRowBad = 0x8000u;    // cnt flag: the row holds an invalid target
 
 // Bytes of the fully-lit bitmap of A axons as staged in shared memory (one
@@ -1113,6 +1143,8 @@ __global__ void __launch_bounds__(LIT ? 1024 : 256, LIT ? 1 : 4)
   __shared__ uint32_t s_pmax;
   __shared__ uint64_t s_bar;
   extern __shared__ __align__(128) uint32_t s_lit[];
+  chain_wait();
+  chain_open();
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
   if (INLINE && lsum_tick(ctl, k)) return;              // k_rows_update_lsum runs this tick
   if (LIT && threadIdx.x == 0) mbar_init(&s_bar, 1);
@@ -1302,6 +1334,8 @@ __global__ void __launch_bounds__(256, kLsumBlocks) k_rows_update_lsum(ShardVram
                                                           const uint8_t* __restrict__ lfz,
                                                           const int2* __restrict__ lsum, ColWT wt,
                                                           const LearnCtl* __restrict__ lc) {
+  chain_wait();
+  chain_open();
   if (lc && lc->mode == 1u && !lc->overflow) return;   // learned engine: this tick runs sparse
   if (!lsum_tick(ctl, k)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ctr[6] += 1;   // ticks on the lit-sum form
@@ -1632,6 +1666,8 @@ __global__ void __launch_bounds__(256) k_rows_fixup(ShardVramPtrs P, uint32_t N,
                                                     const uint32_t* __restrict__ fix, ShardCtl* __restrict__ ctl,
                                                     uint32_t k, const uint32_t* __restrict__ ids,
                                                     uint8_t* __restrict__ out, uint32_t num_outputs, ColWT wt) {
+  chain_wait();
+  chain_open();
   const uint32_t nfix = ctl->fix_count;
   const uint32_t overflow = ctl->fix_overflow;
   {
@@ -1700,6 +1736,8 @@ __global__ void __launch_bounds__(256) k_rows_push(BurstHeads8* __restrict__ hea
                                                    uint32_t N, const uint32_t* __restrict__ ids,
                                                    uint8_t* __restrict__ out, uint32_t num_outputs,
                                                    ShardCtl* __restrict__ ctl, uint32_t k) {
+  chain_wait();
+  chain_open();
   const uint32_t ecount = ctl->eval_count[k & 1];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1782,6 +1820,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
                                                              const uint32_t* __restrict__ xlit) {
   __shared__ uint32_t s_base;
   __shared__ uint32_t s_warp[ITEMS][8];
+  chain_wait();
+  chain_open();
   const uint32_t i0 = blockIdx.x * (256u * ITEMS) + threadIdx.x;
   // all loads first: heads, owners, pending pushes, input bits, timers, constants,
   // and the axons the row layout took as fully lit (xlit, 32 per warp)
@@ -2019,35 +2059,33 @@ static bool rows_lit(uint32_t A) { return (size_t)lit_smem_bytes(A) <= lit_smem_
 
 // inline: GSOP inside the pass (rows with their movable slots first), else
 // the spikers are listed for launch_rows_gsop.
+// pdl: launched into the tick's kernel chain (launch_chain).
 template <bool INLINE>
 static void launch_rows_update(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, uint32_t A, uint32_t k,
-                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream, ColWT wt = ColWT{}) {
+                               uint32_t fix_cap, const LearnCtl* lc, cudaStream_t stream, ColWT wt = ColWT{},
+                               bool pdl = false) {
   RowCache& r = *s.rows;
   const int sms = sm_count();
   const bool lit = rows_lit(A);
   const dim3 grid(lit ? sms : 4 * sms), block(lit ? 1024 : 256);
   const size_t smem = lit ? lit_smem_bytes(A) : 0;
+  auto go = [&](auto kern) {
+    launch_chain(kern, grid, block, smem, stream, pdl, v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
+                 s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n, r.lfz, r.wcnt, wt);
+  };
   if constexpr (INLINE) {
     if (wt.w) {   // the per-tick entry point: weight changes written through
       if (lit)
-        k_rows_update<true, true, true><<<grid, block, smem, stream>>>(
-            v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n,
-            r.gd_n, r.lfz, r.wcnt, wt);
+        go(k_rows_update<true, true, true>);
       else
-        k_rows_update<false, true, true><<<grid, block, smem, stream>>>(
-            v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n,
-            r.gd_n, r.lfz, r.wcnt, wt);
+        go(k_rows_update<false, true, true>);
       return;
     }
   }
   if (lit)
-    k_rows_update<true, INLINE><<<grid, block, smem, stream>>>(
-        v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
-        r.lfz, r.wcnt, wt);
+    go(k_rows_update<true, INLINE>);
   else
-    k_rows_update<false, INLINE><<<grid, block, smem, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend,
-                                                                r.fix, s.ctl, k, fix_cap, r.lit, lc, r.gs_n, r.gd_n,
-                                                                r.lfz, r.wcnt, wt);
+    go(k_rows_update<false, INLINE>);
 }
 
 // The GSOP passes over the spikers the tick's update pass listed (32 warps per
@@ -2088,6 +2126,12 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   if (bitmask && ((uint64_t)a.virtual_offset + a.num_virtual > A)) raise |= AXC_ERR_VIRTUAL_RANGE;
   const uint32_t G = max(A, N);
   const bool per_tick = !a.batch;
+  // The per-tick entry point launches the kernels after the prologue into the
+  // kernel chain (launch_chain), which overlaps each stream launch with the
+  // kernel before it: 4,841 against 4,617 calls/s at 1.5M neurons.  A batch's
+  // captured graph gains nothing from it (16,955 against 17,073 ticks/s) and
+  // keeps plain edges.  Never while stage events are recorded.
+  const bool pdl = per_tick && ev == nullptr;
   if (G)
     k_rows_prologue_plain<kProItems><<<(G + 256 * kProItems - 1) / (256 * kProItems), 256, 0, stream>>>(
         v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
@@ -2106,22 +2150,19 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   // with GSOP; both are launched and each returns at once on the other's
   // ticks), ev[4]..ev[5] fix-up and push.
   const uint32_t fix_cap = min(a.fix_cap, kFixCap);
-  launch_rows_update<true>(v, s, N, A, a.k, fix_cap, nullptr, stream, wt);
+  launch_rows_update<true>(v, s, N, A, a.k, fix_cap, nullptr, stream, wt, pdl && G);
   if (ev) cudaEventRecord(ev[3], stream);
-  if (per_tick)
-    k_rows_update_lsum<true><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                          s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt, nullptr);
-  else
-    k_rows_update_lsum<false><<<kLsumBlocks * sms, 256, 0, stream>>>(v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix,
-                                                           s.ctl, a.k, fix_cap, r.lit, r.lfz, r.lsum, wt, nullptr);
+  launch_chain(per_tick ? k_rows_update_lsum<true> : k_rows_update_lsum<false>, dim3(kLsumBlocks * sms), dim3(256),
+               0, stream, pdl, v, A, r.rt, r.rw, r.cnt, r.mask2, r.eval, s.pend, r.fix, s.ctl, a.k, fix_cap, r.lit,
+               r.lfz, r.lsum, wt, (const LearnCtl*)nullptr);
   if (ev) cudaEventRecord(ev[4], stream);
   const bool readout = a.num_outputs > 0 && a.mapped_soma_ids && a.output_history;
-  k_rows_fixup<<<2 * sms, 256, 0, stream>>>(v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend, r.eval, r.fix, s.ctl, a.k,
-                                            a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0, wt);
+  launch_chain(k_rows_fixup, dim3(2 * sms), dim3(256), 0, stream, pdl, v, N, A, r.rt, r.rw, r.cnt, r.mask2, s.pend,
+               r.eval, r.fix, s.ctl, a.k, a.mapped_soma_ids, a.output_history, readout ? a.num_outputs : 0, wt);
   // the soma pushes: by the next tick's prologue within a batch, here on its last tick
   if (!a.defer_push)
-    k_rows_push<<<2 * sms, 256, 0, stream>>>(v.axon_heads, v.soma_to_axon, A, s.pend, r.eval, v.soma_flags, N,
-                                             nullptr, nullptr, 0, s.ctl, a.k);
+    launch_chain(k_rows_push, dim3(8 * sms), dim3(256), 0, stream, pdl, v.axon_heads, v.soma_to_axon, A, s.pend,
+                 r.eval, v.soma_flags, N, (const uint32_t*)nullptr, (uint8_t*)nullptr, 0u, s.ctl, a.k);
   if (ev) cudaEventRecord(ev[5], stream);
   return cudaGetLastError();
 }

@@ -26,10 +26,25 @@ from axicor_gb300.formats import StateView
 pytestmark = pytest.mark.gpu
 
 
+def mostly_frozen(w, state, N, seed=5, movable=0.04):
+    """Weights at a zero-inertia rank (|w| >= 2048 with inertia_curve[1..] = 0) but for a few percent, so that
+    the layouts meet the lit-sum criterion early and the device keeps the copy between layouts."""
+    for v in (0, 1):
+        w.lut[v]["inertia_curve"] = np.array([128] + [0] * 15, np.uint8)
+    sv = StateView(state, N)
+    rng = np.random.default_rng(seed)
+    live = sv.targets != 0
+    freeze = live & (rng.random(live.shape) >= movable)
+    mag = rng.integers(2048, 3000, size=int(freeze.sum())).astype(np.int16)
+    sv.weights[freeze] = np.where(sv.weights[freeze] < 0, -mag, mag).astype(np.int16)
+
+
 class BatchTwin:
-    def __init__(self, w):
+    def __init__(self, w, frozen=True):
         self.w = w
         self.lay, self.h_state, self.h_heads = S.generate_brain(w.spec())
+        if frozen:
+            mostly_frozen(w, self.h_state, self.lay.padded_n)
         self.N, self.A = self.lay.padded_n, self.lay.total_axons
         S.upload_lut(w.lut)
         self.vram = S.VramState(self.N, self.A)
@@ -86,32 +101,36 @@ def _raw_htod(dev_ptr, host):
 
 
 def test_batches_on_kept_rows_through_relayouts(gpu):
-    """40 batches of 20 ticks with nothing in between, with GSOP still moving weights (several movable
-    inertia ranks): layouts and kept copies alternate as the device decides, every batch bit-exact."""
+    """40 batches of 20 ticks with nothing in between on a brain whose weights are frozen but for 4 %: the
+    layouts meet the lit-sum criterion, so the device keeps the copy for 100 to 800 ticks between layouts,
+    while GSOP keeps moving the movable weights; every batch bit-exact."""
     w = W.small(dims=(16, 16, 8), slots=80, inputs=64, p=0.1)
-    for v in (0, 1):
-        w.lut[v]["inertia_curve"] = np.array([128, 110, 90, 70, 50] + [0] * 11, np.uint8)
     t = BatchTwin(w)
     try:
         w0 = StateView(t.h_state, t.N).weights.copy()
+        t.vram.counters(reset=True)
         for _ in range(40):
             t.batch()
-        assert np.count_nonzero(StateView(t.h_state, t.N).weights != w0) > 1000, "GSOP must move weights"
+        assert np.count_nonzero(StateView(t.h_state, t.N).weights != w0) > 100, "GSOP must move weights"
+        assert t.vram.counters()[6] > 200, "the kept layouts must run the lit-sum form"
         assert t.vram.error_flags() == 0
     finally:
         t.close()
 
 
 def test_batches_follow_every_external_write(gpu):
+    """Between kept copies (a mostly frozen brain, so the device keeps the rows from batch to batch) the shard
+    and the LUT are written by every route the reference uses; each write must send the next batch to a new
+    layout."""
     lib = N.lib()
     w = W.small(dims=(16, 16, 8), slots=80, inputs=64, p=0.1)
-    for v in (0, 1):
-        w.lut[v]["inertia_curve"] = np.array([128, 96, 64, 32] + [0] * 12, np.uint8)
     t = BatchTwin(w)
     rng = np.random.default_rng(17)
     try:
-        for _ in range(3):
+        t.vram.counters(reset=True)
+        for _ in range(6):
             t.batch()
+        assert t.vram.counters()[6] > 0, "the device must keep the copy (lit-sum ticks) before the writes"
         # 1. cu_upload_state_blob with edited weights (boot / checkpoint restore)
         sv = StateView(t.h_state, t.N)
         live = sv.targets != 0
@@ -146,7 +165,7 @@ def test_batches_follow_every_external_write(gpu):
         # 4. a new LUT (other frozen ranks, other lengths)
         lut = t.w.lut.copy()
         for v in (0, 1):
-            lut[v]["inertia_curve"] = np.array([128, 128, 100, 80, 60, 40] + [0] * 10, np.uint8)
+            lut[v]["inertia_curve"] = np.array([128, 128] + [0] * 14, np.uint8)   # the 2048..4095 ranks move again
         lut[1]["signal_propagation_length"] = 3
         t.w.lut = lut
         S.upload_lut(lut)
