@@ -589,15 +589,31 @@ __global__ void __launch_bounds__(256) k_rows_mult(const uint32_t* __restrict__ 
   if (a < A) atomicAdd(&mult[a], 1u);
 }
 
-// batch end: weights rows -> columnar for the slots before the first empty
-// target (slot q of neuron n from row position row_pos of its omask).
+// Batch end: weights rows -> columnar, a thread per neuron.  The k-th set bit
+// of omask[n] (a columnar slot q) is row position k: the row's first group,
+// the only slots whose weights GSOP can have changed.  A neuron without such
+// slots (every neuron of a frozen row) costs one 16-byte load, so in a brain
+// whose weights have mostly frozen the write-back reads 16 bytes a neuron
+// instead of a tile's rows.  Where every slot is movable, neighbouring threads
+// write the same slot of neighbouring neurons: 64 contiguous bytes a warp.
 __global__ void __launch_bounds__(256) k_rows_writeback(int16_t* __restrict__ weights, uint32_t N,
                                                         const int16_t* __restrict__ rw,
-                                                        const uint16_t* __restrict__ cnt,
                                                         const uint4* __restrict__ omask) {
-  __shared__ int16_t s_w[AXC_MAX_DENDRITES][34];
-  __shared__ uint32_t s_c[32];
-  writeback_tile(weights, N, blockIdx.x * 32, rw, cnt, omask, s_w, s_c);
+  const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const uint4 om = omask[n];
+  const uint32_t o[4] = {om.x, om.y, om.z, om.w};
+  const int16_t* row = rw + (size_t)n * kRowStride;
+  uint32_t k = 0;
+#pragma unroll
+  for (int ch = 0; ch < 4; ch++) {
+    uint32_t b = o[ch];
+    while (b) {
+      const uint32_t q = 32u * ch + (uint32_t)(__ffs(b) - 1);
+      b &= b - 1u;
+      weights[(size_t)q * N + n] = row[k++];
+    }
+  }
 }
 
 // Learned engine, in the prologue: per-tile active synapses and heads in
@@ -2169,7 +2185,7 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
 
 cudaError_t launch_rows_end(const ShardVramPtrs& v, ShardScratch& s, uint32_t N, cudaStream_t stream) {
   RowCache& r = *s.rows;
-  if (N) k_rows_writeback<<<(N + 31) / 32, 256, 0, stream>>>(v.dendrite_weights, N, r.rw, r.cnt, r.omask);
+  if (N) k_rows_writeback<<<(N + 255) / 256, 256, 0, stream>>>(v.dendrite_weights, N, r.rw, r.omask);
   return cudaGetLastError();
 }
 
