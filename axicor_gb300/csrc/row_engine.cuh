@@ -1948,8 +1948,11 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
 // Items (an axon and a neuron each) per thread of k_rows_prologue_plain: two
 // halve the blocks, and with them the list-append atomics on one counter and
 // the per-block barriers (1.5M neurons: 18,162 against 17,733 ticks/s; four
-// are slower, 16,717).
-constexpr int kProItems = 2;
+// are slower, 16,717), where the grid at one item has at least kProWide
+// blocks (four waves of 8 blocks per SM on 152 SMs); a smaller brain keeps one
+// item per thread and twice the blocks (16k neurons: 64 blocks, 60,629 ticks/s
+// at two items).
+constexpr uint32_t kProWide = 4864;
 
 }  // namespace
 
@@ -2156,12 +2159,16 @@ cudaError_t launch_tick_rows(const ShardVramPtrs& v, ShardScratch& s, const Tick
   // captured graph gains nothing from it (16,955 against 17,073 ticks/s) and
   // keeps plain edges.  Never while stage events are recorded.
   const bool pdl = per_tick && ev == nullptr;
-  if (G)
-    k_rows_prologue_plain<kProItems><<<(G + 256 * kProItems - 1) / (256 * kProItems), 256, 0, stream>>>(
-        v.axon_heads, A, a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
-        (have_incoming && !per_tick) ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags, v.timers, N,
-        r.eval, s.ctl, raise, r.lit, (a.k > 0 && !per_tick) ? s.pend : nullptr,
-        (have_incoming && per_tick) ? 1u : 0u, per_tick ? 1u : 0u, a.tick - a.k, (int32_t)a.dopamine, r.xlit);
+  if (G) {
+    const bool wide = (G + 255) / 256 >= kProWide;
+    launch_chain(wide ? k_rows_prologue_plain<2> : k_rows_prologue_plain<1>,
+                 dim3(wide ? (G + 511) / 512 : (G + 255) / 256), dim3(256), 0, stream, false, v.axon_heads, A,
+                 a.v_seg, bitmask, a.virtual_offset, a.num_virtual, s.incoming,
+                 (have_incoming && !per_tick) ? s.batch_counts : nullptr, a.k, r.mask2, r.mult, v.soma_flags,
+                 v.timers, N, r.eval, s.ctl, raise, r.lit, (a.k > 0 && !per_tick) ? s.pend : nullptr,
+                 (have_incoming && per_tick) ? 1u : 0u, per_tick ? 1u : 0u, a.tick - a.k, (int32_t)a.dopamine,
+                 r.xlit);
+  }
   if (ev) cudaEventRecord(ev[2], stream);
   ColWT wt{};
   if (per_tick) {
