@@ -52,8 +52,10 @@ constexpr uint32_t kInf = 0xFFFFFFFFu;
 // chain_wait() before it can exit, so a kernel's completion implies its
 // predecessor's, and the chain stays ordered end to end.  chain_open() then
 // lets the next kernel of the chain be scheduled (after this grid's last block
-// started and passed its own wait).  Both are no-ops for a kernel launched
-// without the attribute.
+// started and passed its own wait); it only matters when that kernel is
+// launched with the attribute.  In a kernel launched without it (the prologue,
+// every kernel of a captured batch) chain_wait() returns at once: the stream
+// finished the predecessor before the kernel started.
 __device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void chain_open() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
