@@ -143,7 +143,9 @@ class Clocks:
 
 
 # DRAM traffic per launch of the dominant kernel (ncu dram__bytes_read.sum + dram__bytes_write.sum) from one
-# capture of the same kernel on the same workload in its steady state (tick ~1,200)
+# capture of the same kernel on the same workload in its steady state (tick ~1,200).  The prologue's was
+# taken with one axon and neuron per thread; at this size it now runs two per thread, which move the same
+# bytes.
 TRAFFIC = {("plain-1.5M", "k_rows_update_lsum"): 66.5e6, ("plain-1.5M", "k_rows_prologue_plain"): 66.1e6}
 
 
