@@ -72,6 +72,8 @@ static void launch_chain(void (*kern)(P...), dim3 grid, dim3 block, size_t smem,
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = pdl ? 1 : 0;
+  // a failed launch also leaves its error for cudaGetLastError, which the
+  // launch sequences return
   cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 constexpr uint32_t kRowBad = 0x8000u;    // cnt flag: the row holds an invalid target
@@ -1952,8 +1954,8 @@ __global__ void __launch_bounds__(256) k_rows_prologue_plain(BurstHeads8* __rest
 // the per-block barriers (1.5M neurons: 18,162 against 17,733 ticks/s; four
 // are slower, 16,717), where the grid at one item has at least kProWide
 // blocks (four waves of 8 blocks per SM on 152 SMs); a smaller brain keeps one
-// item per thread and twice the blocks (16k neurons: 64 blocks, 60,629 ticks/s
-// at two items).
+// item per thread and twice the blocks (16k neurons: 66,644 ticks/s with one
+// item and 64 blocks, 60,629 with two and 32).
 constexpr uint32_t kProWide = 4864;
 
 }  // namespace
