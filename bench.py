@@ -359,9 +359,11 @@ def run_gb300(args, dist: Dist) -> dict | None:
         "clocks": clk,
         "h2d": B * words * 4,
         "d2h": B * n_out,
-        # per batch of B ticks: rows: prologue, update, fix-up per tick; push on the last tick;
-        # batch control, burst reset, list reset, owner counts, row copy, write-back
-        "launches": K * ((3 * B + 7) if engine == 1 else (4 * B + 2)),
+        # per batch of B ticks: rows: prologue, 8-lane pass, lit-sum pass, fix-up per tick (one of the two
+        # passes returns at once); push on the last tick; batch control, burst reset, list reset, layout
+        # start, owner counts, row layout (the three layout kernels return at once on batches that keep
+        # the copy), write-back
+        "launches": K * ((4 * B + 8) if engine == 1 else (4 * B + 2)),
         "roofline": {"bound": "hbm", "kernel": kernels.get(names[top], names[top]),
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": TRAFFIC.get((args.workload, kernels.get(names[top], names[top]))),
